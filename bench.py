@@ -1,0 +1,396 @@
+"""Benchmark of the fastreg registration loop on GB300.
+
+One step = one whole registration (fastreg's FastReg::operator()) of the 182x218x182
+synthetic pair for 200 iterations with the reference solver (params.ini values of the
+reference: ALPHA=0.004, TAU=0.2, W_REG=0.2, RHO_0=1, p=2, C=0.25), inputs resident
+in HBM.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference algorithm's CPU implementation (the oracle
+port, OpenMP over all host cores) on a bounded sample of the same workload.
+Multi-GPU runs are independent replicas (one pair per rank, no collective on the
+data path); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "pairs/s at 182×218×182, 200 its, batched vs plain; warp GB/s vs HBM peak"
+DIMS = (182, 218, 182)
+ITERS = 200
+
+# algorithmic bytes per interior voxel and launch (packed FP32: vector 12 B, scalar 4 B)
+BYTES_LAPLACIAN = 12 + 12           # psi read, L written
+BYTES_PASS_A = 4 + 12 + 12 + 12 + 4 + 4 + 4 + 12 + 12  # rho, v, psi_inv, L o psi_inv, S, T o psi_inv; rho, v, psi_inv
+BYTES_PASS_B = 12 + 12 + 12         # psi, v o psi gathered, psi written
+BYTES_ITER_CANONICAL = 112          # per voxel-iteration with L recomputed from psi (no L round trip)
+BYTES_WARP = 12 + 4 + 4 + 2 + 2     # psi, image gathered, out, label gathered, out label
+
+
+def reference_params(dims=DIMS, iters=ITERS, solver="reference"):
+    from fastreg_gb300 import Params
+    return Params(volume_dims=dims, volume_size=(1.0, 1.0, 1.0), no_labels=8, max_iter=iters,
+                  max_update_norm=-1e-10, rho_0=1.0, tau=0.2, w_reg=0.2, alpha=0.004, p=2.0, C=0.25,
+                  reset_iter=-1, verbosity=0, solver=solver, smooth_sigma=1.5, smooth_width=7, damping=0.9,
+                  step=0.5)
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            d = json.loads(p.read_text())
+            return float(d["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def load_traffic(kernel: str):
+    """dram bytes per launch of `kernel` at the bench workload, from the committed ncu
+    summary (a line 'dram_bytes_per_launch_cfg2: <int>'), or None."""
+    f = ROOT / "profiles" / f"{kernel}_cfg2.txt"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_cfg2:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(ws, v):
+    if ws == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference_sample(data, P, sample_iters=(2, 6)):
+    """Time the oracle port (the reference algorithm on the host cores) on the full
+    volume for a few iterations and extrapolate to a whole registration."""
+    from oracle import oracle as O
+    a, b = sample_iters
+    times = {}
+    for n in (a, b):
+        Pn = reference_params(DIMS, n)
+        t0 = time.perf_counter()
+        O.ref_register(Pn, data["T"], data["labT"], data["S"], data["labS"])
+        times[n] = time.perf_counter() - t0
+    per_iter = max((times[b] - times[a]) / (b - a), 1e-9)
+    fixed = max(times[a] - a * per_iter, 0.0)
+    full = fixed + ITERS * per_iter
+    return 1.0 / full, per_iter, times
+
+
+def run_reference_arm(args):
+    ws, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0
+    if rank != 0:
+        return 0
+    from fastreg_gb300 import synthetic as sy
+    from oracle import build as obuild
+    obuild.build()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    data = sy.make_pair(sy.CFG2)
+    P = reference_params()
+    vals = []
+    for step in range(args.warmup + args.steps):
+        v, per_iter, _ = cpu_reference_sample(data, P, sample_iters=(1, 2))
+        if step >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "cfg2: one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
+                   "solver": "reference", "sample": "1 and 2 iterations of the full volume per step, extrapolated "
+                                                   "to 200 iterations"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": "CPU oracle (OpenMP, FP32, op-order matched) on the 182x218x182 pair, 1 and 2 "
+                                   "iterations, extrapolated to 200"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the sobolev/warp/kernel/CPU measurements")
+    ap.add_argument("--profile", action="store_true", help="short run for an ncu launch list")
+    args = ap.parse_args()
+    if args.warmup < 3 and not args.profile:
+        args.warmup = 3
+
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    ws, rank, local = dist_setup()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from fastreg_gb300 import FastReg, synthetic as sy, warp, _native as N
+    import ctypes as C
+
+    spec = sy.CFG2
+    if ws > 1:
+        spec = sy.PairSpec(**{**spec.__dict__, "seed": spec.seed + rank})
+    data = sy.make_pair(spec)
+    P = reference_params()
+    fr = FastReg(P)
+    stream = torch.cuda.Stream(device=dev)
+    pristine = [torch.from_numpy(data[k]).to(dev) for k in ("T", "labT", "S", "labS")]
+    work = [t.clone() for t in pristine]
+
+    def step():
+        for w, p in zip(work, pristine):
+            w.copy_(p, non_blocking=True)
+        fr(*work, stream=stream, sync=False)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    stream.synchronize()
+
+    sampler = ClockSampler(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    barrier(ws)
+    ms = e0.elapsed_time(e1)
+    ms_max = allmax(ws, ms)
+    value = ws * args.steps / (ms_max / 1000.0)
+    st = fr.stats()
+
+    # end to end through the public API with host buffers: H2D of the inputs, the
+    # registration, D2H of the warped images/labels and of the statistics
+    host_in = [t.cpu().pin_memory() for t in pristine]
+    host_out = [torch.empty_like(t).pin_memory() for t in host_in]
+    h2d = sum(t.numel() * t.element_size() for t in host_in)
+    d2h = h2d + C.sizeof(N.fr_stats)
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def e2e_step():
+        for w, h in zip(work, host_in):
+            w.copy_(h, non_blocking=True)
+        fr(*work, stream=stream, sync=False)
+        for h, w in zip(host_out, work):
+            h.copy_(w, non_blocking=True)
+        stream.synchronize()
+        fr.stats()
+
+    with torch.cuda.stream(stream):
+        e2e_step()
+        barrier(ws)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(e2e_steps):
+            e2e_step()
+        e1.record(stream)
+        stream.synchronize()
+        t_e2e = time.perf_counter() - t0
+    e2e_max = allmax(ws, t_e2e)
+    e2e_value = ws * e2e_steps / e2e_max
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded: 400 Gaussian blobs + N(0,0.01), smooth velocity sigma 6, max disp 6, 8 classes)",
+        "config": {"workload": "cfg2: one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
+                   "solver": "reference", "voxels": int(np.prod(DIMS)), "iterations": ITERS,
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+                   "l2": "working set ~0.7 GB per pair, larger than L2 (no flush needed)"},
+        "voxel_iters_per_s": value * int(np.prod(DIMS)) * ITERS,
+        "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": args.steps * (2 + 3 * ITERS),
+        "clocks": clocks,
+        "result": {"iterations": st.iterations, "e_data": st.e_data, "e_reg": st.e_reg, "folds": st.folds,
+                   "dice_all": st.dice_all},
+    }
+
+    if rank == 0 and not args.no_extras and not args.profile:
+        peak, peak_kind = load_peaks()
+        # per-kernel durations (CUDA events around each launch on `stream`)
+        fr.begin([tuple(work)], stream=stream)
+        ms_k = (C.c_float * 8)()
+        nk = C.c_int()
+        N.check(fr.lib.fr_time_kernels(fr.h, 20, ms_k, C.byref(nk), stream.cuda_stream), fr.h, "fr_time_kernels")
+        stream.synchronize()
+        ni = (DIMS[0] - 2) * (DIMS[1] - 2) * (DIMS[2] - 2)
+        kern = {"ref_laplacian_kernel": (ms_k[0], BYTES_LAPLACIAN * ni),
+                "ref_pass_a_kernel": (ms_k[1], BYTES_PASS_A * ni),
+                "ref_pass_b_kernel": (ms_k[2], BYTES_PASS_B * ni)}
+        top = max(kern, key=lambda k: kern[k][0])
+        t_top, b_top = kern[top]
+        achieved = b_top / (t_top * 1e-3) / 1e9
+        traffic = load_traffic(top)
+        line["roofline"] = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                            "algorithmic_bytes_per_launch": b_top}
+        line["kernels_ms"] = {k: v[0] for k, v in kern.items()}
+        line["kernels_gbs"] = {k: v[1] / (v[0] * 1e-3) / 1e9 for k, v in kern.items()}
+        iter_ms = sum(v[0] for v in kern.values())
+        line["iteration"] = {"ms": iter_ms, "canonical_bytes_per_voxel": BYTES_ITER_CANONICAL,
+                             "effective_gbs": BYTES_ITER_CANONICAL * int(np.prod(DIMS)) / (iter_ms * 1e-3) / 1e9}
+
+        # standalone warp (apply): S o psi with the final psi of the registration
+        psi = fr.get_field(N.FR_FIELD_PSI)
+        img, lab = pristine[2], pristine[3]
+        out, out_lab = torch.empty_like(img), torch.empty_like(lab)
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                warp(psi, img, lab, stream=stream, out=out, out_lab=out_lab)
+            w0, w1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            w0.record(stream)
+            for _ in range(20):
+                warp(psi, img, lab, stream=stream, out=out, out_lab=out_lab)
+            w1.record(stream)
+        stream.synchronize()
+        wms = w0.elapsed_time(w1) / 20
+        wgbs = BYTES_WARP * int(np.prod(DIMS)) / (wms * 1e-3) / 1e9
+        line["warp"] = {"ms": wms, "gbs": wgbs, "frac_of_peak": wgbs / peak, "bytes_per_voxel": BYTES_WARP}
+
+        # the sobolev solver (SSD + Gaussian-smoothed gradient + momentum) on the same pair
+        Ps = reference_params(solver="sobolev")
+        frs = FastReg(Ps)
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                for w, p in zip(work, pristine):
+                    w.copy_(p, non_blocking=True)
+                frs(*work, stream=stream, sync=False)
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            for _ in range(3):
+                for w, p in zip(work, pristine):
+                    w.copy_(p, non_blocking=True)
+                frs(*work, stream=stream, sync=False)
+            s1.record(stream)
+        stream.synchronize()
+        sms = s0.elapsed_time(s1) / 3
+        ss = frs.stats()
+        line["sobolev"] = {"value": 1000.0 / sms, "unit": "pairs/s", "ms_per_pair": sms, "e_data": ss.e_data,
+                           "e_data_initial": float(0.5 * ((data["T"].astype(np.float64) -
+                                                           data["S"].astype(np.float64)) ** 2).sum()),
+                           "folds": ss.folds, "dice_all": ss.dice_all}
+        frs.close()
+
+        # CPU baseline: the oracle port on the host cores, bounded sample
+        cores = os.cpu_count() or 1
+        os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+        cpu_v, per_iter, _ = cpu_reference_sample(data, P, sample_iters=(1, 3))
+        line["cpu_baseline"] = {"value": cpu_v, "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": "CPU oracle (OpenMP, FP32) on the 182x218x182 pair, 1 and 3 iterations, "
+                                          f"extrapolated to 200 ({per_iter * 1e3:.1f} ms/iteration)"}
+
+    if rank == 0:
+        print(json.dumps(line))
+    fr.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

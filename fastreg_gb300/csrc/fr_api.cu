@@ -1,0 +1,1040 @@
+// fr_api.cu -- host side of the C ABI (include/fastreg_gb300.h).
+//
+// A handle owns one packed cohort of pairs on the device (one allocation carved into
+// fields), the tile table the kernels walk, and a CUDA graph holding every iteration
+// of a registration.  fr_register is fr_register_batch with one pair.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cctype>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "../../include/fastreg_gb300.h"
+#include "fr_kernels.h"
+#include "fr_sob.h"
+
+using frg::Pair;
+using frg::Tile;
+
+struct fr_handle {
+    fr_params P;
+    std::string err;
+    int device = 0;
+    int num_sms = 0;
+
+    // cohort
+    std::vector<std::array<int, 3>> dims;
+    int npairs = 0;
+    long long NT = 0;
+    std::vector<Pair> hpairs;
+    std::vector<Tile> htiles;
+    std::vector<fr_pair> io;  // caller buffers of the current registration
+
+    // device memory
+    char* block = nullptr;
+    size_t block_bytes = 0;
+    Pair* d_pairs = nullptr;
+    Tile* d_tiles = nullptr;
+    frg::PairIO* d_io = nullptr;
+    float *S = nullptr, *T = nullptr;
+    int16_t *labS = nullptr, *labT = nullptr;
+    float *rho[2] = {nullptr, nullptr}, *v[2] = {nullptr, nullptr}, *pinv[2] = {nullptr, nullptr};
+    float *psi = nullptr, *L = nullptr;
+    int* stop = nullptr;
+    unsigned long long* keys = nullptr;
+    unsigned long long* trace = nullptr;
+    unsigned int* counter = nullptr;
+    double* tile_partials = nullptr;
+    long long* tile_folds = nullptr;
+    unsigned long long* dice = nullptr;
+    double* pair_energy = nullptr;
+    long long* pair_folds = nullptr;
+    int trace_cap = 0;  // iterations the trace array holds
+
+    // sobolev-mode scratch
+    float* grad = nullptr;  // unsmoothed gradient / smoothing temporaries (3 planes x 2)
+    double* sob_energy = nullptr;
+
+    // launch shape
+    int grid_lap = 0, grid_a = 0, grid_b = 0, grid_io = 0;
+
+    // graph of all iterations of a registration
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_valid = false;
+
+    // bookkeeping
+    int last_iter = 0;      // iterations enqueued in the current registration
+    bool have_state = false;
+    bool finished = false;
+    bool stats_ready = false;
+    std::vector<fr_stats> stats;
+    cudaStream_t last_stream = nullptr;
+};
+
+namespace {
+
+int fail(fr_handle* h, int code, const char* fmt, ...) {
+    if (h) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        h->err = buf;
+    }
+    return code;
+}
+
+#define FR_CUDA(h, call)                                                                              \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail((h), FR_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),    \
+                        __FILE__, __LINE__);                                                          \
+    } while (0)
+
+#define FR_LAUNCHED(h)                                                                                 \
+    do {                                                                                              \
+        cudaError_t e_ = cudaGetLastError();                                                          \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail((h), FR_ERR_CUDA, "kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), \
+                        __FILE__, __LINE__);                                                          \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// t for every iteration: t = alpha, then t += alpha with the RESET_ITER restart
+// (solver.cu:327-328,428-432)
+std::vector<float> t_schedule(const fr_params& P) {
+    std::vector<float> ts;
+    ts.reserve(std::max(P.max_iter, 0));
+    float t = P.alpha;
+    for (int iter = 1; iter <= P.max_iter; ++iter) {
+        ts.push_back(t);
+        int next = iter + 1;
+        t += P.alpha;
+        if (P.reset_iter > 0 && next % P.reset_iter == 0) t = P.alpha;
+    }
+    return ts;
+}
+
+int check_params(fr_handle* h, const fr_params* p) {
+    if (!p) return fail(h, FR_ERR_INVALID_ARG, "params is NULL");
+    for (int c = 0; c < 3; ++c)
+        if (p->volume_dims[c] < 1) return fail(h, FR_ERR_INVALID_ARG, "volume_dims[%d] = %d < 1", c, p->volume_dims[c]);
+    if (p->no_labels < 1 || p->no_labels > FR_MAX_LABELS)
+        return fail(h, FR_ERR_INVALID_ARG, "no_labels = %d outside [1, %d]", p->no_labels, FR_MAX_LABELS);
+    if (p->max_iter < 0) return fail(h, FR_ERR_INVALID_ARG, "max_iter = %d < 0", p->max_iter);
+    if (p->solver != FR_SOLVER_REFERENCE && p->solver != FR_SOLVER_SOBOLEV)
+        return fail(h, FR_ERR_INVALID_ARG, "unknown solver %d", p->solver);
+    if (p->solver == FR_SOLVER_REFERENCE && !(p->alpha > 0.f))
+        return fail(h, FR_ERR_INVALID_ARG, "alpha must be > 0 (t starts at alpha)");
+    if (p->solver == FR_SOLVER_SOBOLEV) {
+        if (p->smooth_width < 1 || p->smooth_width > frg::kMaxSmoothWidth || (p->smooth_width & 1) == 0)
+            return fail(h, FR_ERR_INVALID_ARG, "smooth_width = %d must be odd and in [1, %d]", p->smooth_width,
+                        frg::kMaxSmoothWidth);
+        if (!(p->smooth_sigma > 0.f)) return fail(h, FR_ERR_INVALID_ARG, "smooth_sigma must be > 0");
+    }
+    if (p->verbosity < 0 || p->verbosity > 2) return fail(h, FR_ERR_INVALID_ARG, "verbosity must be 0, 1 or 2");
+    return FR_OK;
+}
+
+int occupancy_grid(fr_handle* h, const void* fn, int ntiles) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    long long g = (long long)per_sm * h->num_sms;
+    return (int)std::max(1LL, std::min<long long>(g, ntiles));
+}
+
+void release(fr_handle* h) {
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    h->graph_valid = false;
+    if (h->block) cudaFree(h->block);
+    h->block = nullptr;
+    h->block_bytes = 0;
+    h->npairs = 0;
+    h->dims.clear();
+    h->have_state = false;
+}
+
+// (Re)build the packed cohort for the given pair sizes.
+int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
+    std::vector<std::array<int, 3>> dims(n);
+    for (int p = 0; p < n; ++p) {
+        for (int c = 0; c < 3; ++c) {
+            if (pairs[p].dims[c] < 4)
+                return fail(h, FR_ERR_INVALID_ARG, "pair %d dims[%d] = %d < 4 (the solver needs an interior)", p, c,
+                            pairs[p].dims[c]);
+            dims[p][c] = pairs[p].dims[c];
+        }
+        long long N = (long long)dims[p][0] * dims[p][1] * dims[p][2];
+        if (N > 0xfffffffeLL) return fail(h, FR_ERR_INVALID_ARG, "pair %d has %lld voxels (limit 2^32-2)", p, N);
+    }
+    const int want_trace = std::max(h->P.max_iter, 1);
+    if (h->block && dims == h->dims && h->trace_cap >= want_trace) return FR_OK;
+    release(h);
+
+    h->dims = dims;
+    h->npairs = n;
+    h->hpairs.assign(n, Pair{});
+    h->htiles.clear();
+    long long off = 0;
+    for (int p = 0; p < n; ++p) {
+        Pair& P = h->hpairs[p];
+        P.X = dims[p][0];
+        P.Y = dims[p][1];
+        P.Z = dims[p][2];
+        P.N = (long long)P.X * P.Y * P.Z;
+        P.off = off;
+        off += (long long)align_up((size_t)P.N, 32);
+        const int tz = h->P.solver == FR_SOLVER_SOBOLEV ? frg::kSobTileZ : frg::kTileZ;
+        const int ty = h->P.solver == FR_SOLVER_SOBOLEV ? frg::kSobTileY : frg::kTileY;
+        for (int z0 = 0; z0 < P.Z; z0 += tz)
+            for (int y0 = 0; y0 < P.Y; y0 += ty)
+                for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) h->htiles.push_back(make_int4(p, x0, y0, z0));
+    }
+    h->NT = std::max(off, 32LL);
+    const long long NT = h->NT;
+    const int ntiles = (int)h->htiles.size();
+    h->trace_cap = want_trace;
+
+    // carve one allocation
+    struct Slot {
+        void** ptr;
+        size_t bytes;
+    };
+    std::vector<Slot> slots;
+    auto add = [&](void** p, size_t bytes) { slots.push_back({p, bytes}); };
+    add((void**)&h->d_pairs, sizeof(Pair) * n);
+    add((void**)&h->d_tiles, sizeof(Tile) * ntiles);
+    add((void**)&h->d_io, sizeof(frg::PairIO) * n);
+    add((void**)&h->S, sizeof(float) * NT);
+    add((void**)&h->T, sizeof(float) * NT);
+    add((void**)&h->labS, sizeof(int16_t) * NT);
+    add((void**)&h->labT, sizeof(int16_t) * NT);
+    add((void**)&h->psi, sizeof(float) * 3 * NT);
+    add((void**)&h->v[0], sizeof(float) * 3 * NT);
+    add((void**)&h->v[1], sizeof(float) * 3 * NT);
+    if (h->P.solver == FR_SOLVER_REFERENCE) {
+        add((void**)&h->rho[0], sizeof(float) * NT);
+        add((void**)&h->rho[1], sizeof(float) * NT);
+        add((void**)&h->pinv[0], sizeof(float) * 3 * NT);
+        add((void**)&h->pinv[1], sizeof(float) * 3 * NT);
+        add((void**)&h->L, sizeof(float) * 3 * NT);
+    } else {
+        h->rho[0] = h->rho[1] = h->pinv[0] = h->pinv[1] = h->L = nullptr;
+        add((void**)&h->grad, sizeof(float) * 3 * NT);
+        add((void**)&h->sob_energy, sizeof(double) * (size_t)n * want_trace);
+    }
+    add((void**)&h->stop, sizeof(int) * n);
+    add((void**)&h->keys, sizeof(unsigned long long) * n);
+    add((void**)&h->trace, sizeof(unsigned long long) * (size_t)n * want_trace);
+    add((void**)&h->counter, sizeof(unsigned int) * 4);
+    add((void**)&h->tile_partials, sizeof(double) * 2 * ntiles);
+    add((void**)&h->tile_folds, sizeof(long long) * ntiles);
+    add((void**)&h->dice, sizeof(unsigned long long) * (size_t)n * (2 * 256 + 1));
+    add((void**)&h->pair_energy, sizeof(double) * 2 * n);
+    add((void**)&h->pair_folds, sizeof(long long) * n);
+    size_t total = 0;
+    for (auto& s : slots) total = align_up(total, 256) + s.bytes;
+    total = align_up(total, 256);
+    cudaError_t e = cudaMalloc((void**)&h->block, total);
+    if (e != cudaSuccess) {
+        h->block = nullptr;
+        cudaGetLastError();
+        h->dims.clear();
+        return fail(h, FR_ERR_ALLOC, "cudaMalloc of %zu bytes for %d pair(s) failed: %s", total, n,
+                    cudaGetErrorString(e));
+    }
+    h->block_bytes = total;
+    size_t at = 0;
+    for (auto& s : slots) {
+        at = align_up(at, 256);
+        *s.ptr = h->block + at;
+        at += s.bytes;
+    }
+    // everything starts at zero: L's boundary shell, counters, partials
+    FR_CUDA(h, cudaMemset(h->block, 0, total));
+    FR_CUDA(h, cudaMemcpy(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice));
+    FR_CUDA(h, cudaMemcpy(h->d_tiles, h->htiles.data(), sizeof(Tile) * ntiles, cudaMemcpyHostToDevice));
+
+    if (h->P.solver == FR_SOLVER_REFERENCE) {
+        h->grid_lap = occupancy_grid(h, (const void*)frg::ref_laplacian_kernel, ntiles);
+        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, ntiles);
+        h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, ntiles);
+    } else {
+        h->grid_a = occupancy_grid(h, (const void*)frg::sob_grad_kernel, ntiles);
+        h->grid_lap = occupancy_grid(h, (const void*)frg::sob_smooth_kernel, ntiles);
+        h->grid_b = occupancy_grid(h, (const void*)frg::sob_pass_b_kernel, ntiles);
+    }
+    h->grid_io = occupancy_grid(h, (const void*)frg::finalize_kernel, ntiles);
+    return FR_OK;
+}
+
+frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
+    frg::RefIterArgs a{};
+    a.pairs = h->d_pairs;
+    a.tiles = h->d_tiles;
+    a.ntiles = (int)h->htiles.size();
+    a.npairs = h->npairs;
+    a.NT = h->NT;
+    a.S = h->S;
+    a.T = h->T;
+    const int src = (iter - 1) & 1, dst = iter & 1;
+    a.rho = h->rho[src];
+    a.v = h->v[src];
+    a.pinv = h->pinv[src];
+    a.rho_n = h->rho[dst];
+    a.v_n = h->v[dst];
+    a.pinv_n = h->pinv[dst];
+    a.psi = h->psi;
+    a.L = h->L;
+    const fr_params& P = h->P;
+    // solver.cu:198-199, evaluated once per iteration on the host in float
+    const float m1 = P.p + 1.f;
+    a.alpha = P.alpha;
+    a.f1 = m1 / t;
+    a.m2 = (P.C * powf(P.p, 2.f)) * powf(t, P.p - 2.f);
+    a.tau = P.tau;
+    a.w_reg = P.w_reg;
+    a.max_update_norm = P.max_update_norm;
+    a.iter = iter;
+    a.first_iter = iter == 1;
+    a.stop = h->stop;
+    a.keys = h->keys;
+    a.trace = h->trace;
+    a.counter = h->counter;
+    return a;
+}
+
+int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev) {
+    frg::RefIterArgs a = ref_args(h, iter, t);
+    if (ev) cudaEventRecord(ev[0], s);
+    frg::ref_laplacian_kernel<<<h->grid_lap, 256, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[1], s);
+    frg::ref_pass_a_kernel<<<h->grid_a, 256, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[2], s);
+    frg::ref_pass_b_kernel<<<h->grid_b, 256, 0, s>>>(a);
+    if (ev) cudaEventRecord(ev[3], s);
+    FR_LAUNCHED(h);
+    return FR_OK;
+}
+
+// kernels launched per iteration
+int kernels_per_iter(const fr_handle* h) { return h->P.solver == FR_SOLVER_REFERENCE ? 3 : 5; }
+
+int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev = nullptr) {
+    if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
+    frg::SobIterArgs a{};
+    a.pairs = h->d_pairs;
+    a.tiles = h->d_tiles;
+    a.ntiles = (int)h->htiles.size();
+    a.npairs = h->npairs;
+    a.NT = h->NT;
+    a.S = h->S;
+    a.T = h->T;
+    a.phi = h->psi;
+    a.m = h->v[0];
+    a.g = h->grad;
+    a.tmp = h->v[1];
+    a.damping = h->P.damping;
+    a.step = h->P.step;
+    frg::gaussian_taps(h->P.smooth_sigma, h->P.smooth_width, a.taps);
+    a.radius = h->P.smooth_width / 2;
+    a.max_update_norm = h->P.max_update_norm;
+    a.iter = iter;
+    a.stop = h->stop;
+    a.keys = h->keys;
+    a.trace = h->trace;
+    a.energy = h->sob_energy;
+    a.counter = h->counter;
+    const int grids[3] = {h->grid_a, h->grid_lap, h->grid_b};
+    cudaError_t e = frg::launch_sob_iter(a, grids, s, ev);
+    if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "sobolev launch failed: %s", cudaGetErrorString(e));
+    return FR_OK;
+}
+
+frg::IoArgs io_args(fr_handle* h) {
+    frg::IoArgs a{};
+    a.pairs = h->d_pairs;
+    a.tiles = h->d_tiles;
+    a.ntiles = (int)h->htiles.size();
+    a.npairs = h->npairs;
+    a.NT = h->NT;
+    a.io = h->d_io;
+    a.S = h->S;
+    a.T = h->T;
+    a.labS = h->labS;
+    a.labT = h->labT;
+    a.rho0 = h->rho[0];
+    a.rho1 = h->rho[1];
+    a.v0 = h->v[0];
+    a.v1 = h->v[1];
+    a.psi = h->psi;
+    a.pinv0 = h->pinv[0];
+    a.pinv1 = h->pinv[1];
+    a.rho_init = h->P.rho_0;
+    a.keep_state = h->P.keep_state && h->have_state;
+    a.sobolev = h->P.solver == FR_SOLVER_SOBOLEV;
+    a.stop = h->stop;
+    a.max_iter = h->last_iter;
+    a.no_labels = h->P.no_labels;
+    a.tile_partials = h->tile_partials;
+    a.tile_folds = h->tile_folds;
+    a.dice = h->dice;
+    a.pair_energy = h->pair_energy;
+    a.pair_folds = h->pair_folds;
+    a.counter = h->counter + 1;
+    a.write_outputs = 1;
+    return a;
+}
+
+// Move each pair's final state into buffer 0 so that a KEEP_STATE call starts from it.
+int normalise_parity(fr_handle* h) {
+    if (h->P.solver != FR_SOLVER_REFERENCE || !h->have_state) return FR_OK;
+    std::vector<int> stop(h->npairs);
+    FR_CUDA(h, cudaDeviceSynchronize());
+    FR_CUDA(h, cudaMemcpy(stop.data(), h->stop, sizeof(int) * h->npairs, cudaMemcpyDeviceToHost));
+    for (int p = 0; p < h->npairs; ++p) {
+        int done = stop[p] ? stop[p] : h->last_iter;
+        if (!(done & 1)) continue;
+        const Pair& P = h->hpairs[p];
+        FR_CUDA(h, cudaMemcpy(h->rho[0] + P.off, h->rho[1] + P.off, sizeof(float) * P.N, cudaMemcpyDeviceToDevice));
+        for (int c = 0; c < 3; ++c) {
+            FR_CUDA(h, cudaMemcpy(h->v[0] + c * h->NT + P.off, h->v[1] + c * h->NT + P.off, sizeof(float) * P.N,
+                                  cudaMemcpyDeviceToDevice));
+            FR_CUDA(h, cudaMemcpy(h->pinv[0] + c * h->NT + P.off, h->pinv[1] + c * h->NT + P.off,
+                                  sizeof(float) * P.N, cudaMemcpyDeviceToDevice));
+        }
+    }
+    return FR_OK;
+}
+
+int host_stats(fr_handle* h);
+
+int verbose_energy(fr_handle* h, int iter, cudaStream_t s, double* energy) {
+    frg::IoArgs a = io_args(h);
+    a.write_outputs = 0;
+    a.max_iter = iter - 1;  // state after iter-1 iterations
+    if (h->P.solver == FR_SOLVER_SOBOLEV) a.sobolev = 1;
+    FR_CUDA(h, cudaMemsetAsync(h->dice, 0, sizeof(unsigned long long) * h->npairs * (2 * 256 + 1), s));
+    frg::finalize_kernel<<<h->grid_io, 256, 0, s>>>(a);
+    FR_LAUNCHED(h);
+    std::vector<double> e(2 * h->npairs);
+    FR_CUDA(h, cudaMemcpyAsync(e.data(), h->pair_energy, sizeof(double) * 2 * h->npairs, cudaMemcpyDeviceToHost, s));
+    FR_CUDA(h, cudaStreamSynchronize(s));
+    for (int p = 0; p < h->npairs; ++p) {
+        double val = e[2 * p] + (double)h->P.w_reg * e[2 * p + 1];
+        printf("data energy + w_reg * reg energy = %g + %g * %g = %g\n", e[2 * p], (double)h->P.w_reg, e[2 * p + 1],
+               val);
+        if (p == 0) *energy = val;
+    }
+    return FR_OK;
+}
+
+int run_registration(fr_handle* h, cudaStream_t s) {
+    const fr_params& P = h->P;
+    std::vector<float> ts = t_schedule(P);
+    h->last_iter = P.max_iter;
+    if (P.verbosity == 0) {
+        if (P.max_iter > 0) {
+            if (!h->graph_valid) {
+                if (!h->cap_stream) FR_CUDA(h, cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking));
+                FR_CUDA(h, cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal));
+                int rc = FR_OK;
+                for (int it = 1; it <= P.max_iter && rc == FR_OK; ++it) rc = launch_iter(h, it, ts[it - 1], h->cap_stream);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(h->cap_stream, &g);
+                if (rc != FR_OK) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+                if (h->graph) cudaGraphExecDestroy(h->graph);
+                h->graph = nullptr;
+                e = cudaGraphInstantiate(&h->graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+                h->graph_valid = true;
+            }
+            FR_CUDA(h, cudaGraphLaunch(h->graph, s));
+        }
+        return FR_OK;
+    }
+    // verbose: host-driven loop with the reference's prints (solver.cu:329-433)
+    std::vector<int> stop(h->npairs, 0);
+    for (int iter = 1; iter <= P.max_iter; ++iter) {
+        if (iter == 1 || iter % 100 == 0) printf("iter. no. %d\n", iter);
+        bool report = (P.verbosity == 1 && (iter == 1 || iter % 100 == 0 || iter == P.max_iter)) || P.verbosity == 2;
+        if (report) {
+            double e = 0.0;
+            int rc = verbose_energy(h, iter, s, &e);
+            if (rc != FR_OK) return rc;
+            if (std::isnan(e)) {
+                h->last_iter = iter - 1;
+                return fail(h, FR_ERR_NUMERIC, "energy is NaN at iteration %d", iter);
+            }
+        }
+        int rc = launch_iter(h, iter, ts[iter - 1], s);
+        if (rc != FR_OK) return rc;
+        std::vector<unsigned long long> k(h->npairs);
+        FR_CUDA(h, cudaMemcpyAsync(k.data(), h->trace + (size_t)(iter - 1) * h->npairs,
+                                   sizeof(unsigned long long) * h->npairs, cudaMemcpyDeviceToHost, s));
+        FR_CUDA(h, cudaMemcpyAsync(stop.data(), h->stop, sizeof(int) * h->npairs, cudaMemcpyDeviceToHost, s));
+        FR_CUDA(h, cudaStreamSynchronize(s));
+        if (report) {
+            unsigned bits = (unsigned)(k[0] >> 32);
+            float mx;
+            std::memcpy(&mx, &bits, 4);
+            long long idx = bits ? (long long)(0xffffffffu - (unsigned)(k[0] & 0xffffffffu)) : 0;
+            const Pair& P0 = h->hpairs[0];
+            long long zz = idx / ((long long)P0.X * P0.Y);
+            long long yy = (idx - zz * P0.X * P0.Y) / P0.X;
+            long long xx = idx - P0.X * (yy + (long long)P0.Y * zz);
+            printf("max. update norm %g at voxel (%lld, %lld, %lld)\n", (double)mx, xx, yy, zz);
+        }
+        bool all_stopped = true;
+        for (int p = 0; p < h->npairs; ++p) all_stopped = all_stopped && stop[p] != 0;
+        if (all_stopped) {
+            printf("SOLVER CONVERGED AFTER %d ITERATIONS\n", iter);
+            h->last_iter = iter;
+            return FR_OK;
+        }
+        if (iter == P.max_iter) printf("SOLVER REACHED MAX. NO. OF ITERATIONS WITHOUT CONVERGING\n");
+    }
+    return FR_OK;
+}
+
+int begin(fr_handle* h, const fr_pair* pairs, int n, cudaStream_t s) {
+    if (!pairs || n < 1) return fail(h, FR_ERR_INVALID_ARG, "need at least one pair");
+    for (int p = 0; p < n; ++p)
+        if (!pairs[p].img_T || !pairs[p].lab_T || !pairs[p].img_S || !pairs[p].lab_S)
+            return fail(h, FR_ERR_INVALID_ARG, "pair %d has a NULL buffer", p);
+    bool same = h->block && (int)h->dims.size() == n;
+    for (int p = 0; same && p < n; ++p)
+        for (int c = 0; c < 3; ++c) same = same && h->dims[p][c] == pairs[p].dims[c];
+    if (h->P.keep_state && same && h->have_state) {
+        int rc = normalise_parity(h);
+        if (rc != FR_OK) return rc;
+    }
+    int rc = setup_cohort(h, pairs, n);
+    if (rc != FR_OK) return rc;
+    if (!same) h->have_state = false;
+    h->io.assign(pairs, pairs + n);
+    std::vector<frg::PairIO> io(n);
+    for (int p = 0; p < n; ++p) io[p] = frg::PairIO{pairs[p].img_T, pairs[p].lab_T, pairs[p].img_S, pairs[p].lab_S};
+    FR_CUDA(h, cudaMemcpyAsync(h->d_io, io.data(), sizeof(frg::PairIO) * n, cudaMemcpyHostToDevice, s));
+    FR_CUDA(h, cudaMemsetAsync(h->stop, 0, sizeof(int) * n, s));
+    FR_CUDA(h, cudaMemsetAsync(h->keys, 0, sizeof(unsigned long long) * n, s));
+    FR_CUDA(h, cudaMemsetAsync(h->trace, 0, sizeof(unsigned long long) * n * (size_t)h->trace_cap, s));
+    if (h->sob_energy)
+        FR_CUDA(h, cudaMemsetAsync(h->sob_energy, 0, sizeof(double) * n * (size_t)h->trace_cap, s));
+    frg::IoArgs a = io_args(h);
+    frg::pack_init_kernel<<<h->grid_io, 256, 0, s>>>(a);
+    FR_LAUNCHED(h);
+    h->have_state = true;
+    h->finished = false;
+    h->stats_ready = false;
+    h->last_iter = 0;
+    h->last_stream = s;
+    return FR_OK;
+}
+
+int finish(fr_handle* h, cudaStream_t s) {
+    FR_CUDA(h, cudaMemsetAsync(h->dice, 0, sizeof(unsigned long long) * h->npairs * (2 * 256 + 1), s));
+    frg::IoArgs a = io_args(h);
+    frg::finalize_kernel<<<h->grid_io, 256, 0, s>>>(a);
+    FR_LAUNCHED(h);
+    h->finished = true;
+    h->last_stream = s;
+    return FR_OK;
+}
+
+int host_stats(fr_handle* h) {
+    if (h->stats_ready) return FR_OK;
+    const int n = h->npairs;
+    FR_CUDA(h, cudaStreamSynchronize(h->last_stream));
+    std::vector<int> stop(n);
+    std::vector<double> energy(2 * n);
+    std::vector<long long> folds(n);
+    std::vector<unsigned long long> dice((size_t)n * (2 * 256 + 1));
+    std::vector<unsigned long long> trace((size_t)n * h->trace_cap);
+    FR_CUDA(h, cudaMemcpy(stop.data(), h->stop, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    FR_CUDA(h, cudaMemcpy(energy.data(), h->pair_energy, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
+    FR_CUDA(h, cudaMemcpy(folds.data(), h->pair_folds, sizeof(long long) * n, cudaMemcpyDeviceToHost));
+    FR_CUDA(h, cudaMemcpy(dice.data(), h->dice, sizeof(unsigned long long) * dice.size(), cudaMemcpyDeviceToHost));
+    FR_CUDA(h, cudaMemcpy(trace.data(), h->trace, sizeof(unsigned long long) * trace.size(), cudaMemcpyDeviceToHost));
+    h->stats.assign(n, fr_stats{});
+    for (int p = 0; p < n; ++p) {
+        fr_stats& st = h->stats[p];
+        st.converged = stop[p] != 0;
+        st.iterations = stop[p] ? stop[p] : h->last_iter;
+        if (st.iterations > 0) {
+            unsigned long long k = trace[(size_t)(st.iterations - 1) * n + p];
+            unsigned bits = (unsigned)(k >> 32);
+            std::memcpy(&st.last_max_update_norm, &bits, 4);
+            st.last_max_update_voxel = bits ? (int64_t)(0xffffffffu - (unsigned)(k & 0xffffffffu)) : 0;
+        }
+        st.e_data = energy[2 * p];
+        st.e_reg = energy[2 * p + 1];
+        st.energy = st.e_data + (double)h->P.w_reg * st.e_reg;
+        st.folds = folds[p];
+        st.no_labels = h->P.no_labels;
+        const unsigned long long* dp = dice.data() + (size_t)p * (2 * 256 + 1);
+        double num = 0.0, den = 0.0;
+        for (int l = 0; l < FR_MAX_LABELS; ++l) {
+            st.dice_inter[l] = (int64_t)dp[l];
+            st.dice_count[l] = (int64_t)dp[256 + l];
+            st.dice[l] = dp[256 + l] ? 2.0 * (double)dp[l] / (double)dp[256 + l] : NAN;
+            if (l >= 1 && l < h->P.no_labels) {
+                num += (double)dp[l];
+                den += (double)dp[256 + l];
+            }
+        }
+        st.dice_all = den > 0 ? 2.0 * num / den : NAN;
+        st.dice_out_of_range = (int64_t)dp[2 * 256];
+    }
+    h->stats_ready = true;
+    return FR_OK;
+}
+
+// params.ini: KEY=VALUE lines, '#' comments (boost::program_options::parse_config_file
+// syntax as used by demo.cpp:144-149)
+int set_key(fr_params* p, const std::string& key, const std::string& val, std::string* why) {
+    auto as_int = [&](int* dst) -> bool {
+        char* end = nullptr;
+        long v = strtol(val.c_str(), &end, 10);
+        if (!end || *end != '\0' || val.empty()) return false;
+        *dst = (int)v;
+        return true;
+    };
+    auto as_float = [&](float* dst) -> bool {
+        char* end = nullptr;
+        float v = strtof(val.c_str(), &end);
+        if (!end || *end != '\0' || val.empty()) return false;
+        *dst = v;
+        return true;
+    };
+    bool ok = true;
+    if (key == "VOL_DIMS_X") ok = as_int(&p->volume_dims[0]);
+    else if (key == "VOL_DIMS_Y") ok = as_int(&p->volume_dims[1]);
+    else if (key == "VOL_DIMS_Z") ok = as_int(&p->volume_dims[2]);
+    else if (key == "VOL_SIZE_X") ok = as_float(&p->volume_size[0]);
+    else if (key == "VOL_SIZE_Y") ok = as_float(&p->volume_size[1]);
+    else if (key == "VOL_SIZE_Z") ok = as_float(&p->volume_size[2]);
+    else if (key == "NO_LABELS") ok = as_int(&p->no_labels);
+    else if (key == "MAX_ITER") ok = as_int(&p->max_iter);
+    else if (key == "MAX_UPDATE_NORM") ok = as_float(&p->max_update_norm);
+    else if (key == "RHO_0") ok = as_float(&p->rho_0);
+    else if (key == "RESET_ITER") ok = as_int(&p->reset_iter);
+    else if (key == "TAU") ok = as_float(&p->tau);
+    else if (key == "ALPHA") ok = as_float(&p->alpha);
+    else if (key == "W_REG") ok = as_float(&p->w_reg);
+    else if (key == "p") ok = as_float(&p->p);
+    else if (key == "C") ok = as_float(&p->C);
+    else if (key == "VERBOSITY") ok = as_int(&p->verbosity);
+    else if (key == "SOLVER") {
+        if (val == "reference") p->solver = FR_SOLVER_REFERENCE;
+        else if (val == "sobolev") p->solver = FR_SOLVER_SOBOLEV;
+        else ok = false;
+    } else if (key == "SMOOTH_SIGMA") ok = as_float(&p->smooth_sigma);
+    else if (key == "SMOOTH_WIDTH") ok = as_int(&p->smooth_width);
+    else if (key == "DAMPING") ok = as_float(&p->damping);
+    else if (key == "STEP") ok = as_float(&p->step);
+    else if (key == "KEEP_STATE") ok = as_int(&p->keep_state);
+    else {
+        *why = "unrecognised option '" + key + "'";
+        return FR_ERR_PARSE;
+    }
+    if (!ok) {
+        *why = "bad value '" + val + "' for '" + key + "'";
+        return FR_ERR_PARSE;
+    }
+    return FR_OK;
+}
+
+std::string trim(const std::string& s) {
+    size_t a = 0, b = s.size();
+    while (a < b && std::isspace((unsigned char)s[a])) ++a;
+    while (b > a && std::isspace((unsigned char)s[b - 1])) --b;
+    return s.substr(a, b - a);
+}
+
+thread_local std::string g_parse_error;
+
+}  // namespace
+
+extern "C" {
+
+int fr_abi_version(void) { return FR_ABI_VERSION; }
+
+const char* fr_status_string(int status) {
+    switch (status) {
+        case FR_OK: return "ok";
+        case FR_ERR_INVALID_ARG: return "invalid argument";
+        case FR_ERR_CUDA: return "CUDA error";
+        case FR_ERR_ALLOC: return "allocation failed";
+        case FR_ERR_IO: return "I/O error";
+        case FR_ERR_PARSE: return "parse error";
+        case FR_ERR_STATE: return "call out of order";
+        case FR_ERR_NUMERIC: return "NaN/Inf in the solver";
+        default: return "unknown status";
+    }
+}
+
+const char* fr_last_error(const fr_handle* h) {
+    if (!h) return g_parse_error.c_str();
+    return h->err.c_str();
+}
+
+int fr_params_default(fr_params* p) {
+    if (!p) return FR_ERR_INVALID_ARG;
+    std::memset(p, 0, sizeof(*p));
+    // values of the reference's params.ini (params.ini:1-25); Params defaults
+    // reset_iter = -1, verbosity = 0 (params.hpp:11-12)
+    p->volume_dims[0] = 193;
+    p->volume_dims[1] = 229;
+    p->volume_dims[2] = 193;
+    p->volume_size[0] = p->volume_size[1] = p->volume_size[2] = 1.f;
+    p->no_labels = 6;
+    p->alpha = 0.004f;
+    p->max_iter = 2048;
+    p->max_update_norm = -1e-10f;
+    p->rho_0 = 1.f;
+    p->tau = 0.2f;
+    p->w_reg = 0.2f;
+    p->reset_iter = -1;
+    p->p = 2.f;
+    p->C = 0.25f;
+    p->verbosity = 0;
+    p->solver = FR_SOLVER_REFERENCE;
+    p->smooth_sigma = 1.5f;
+    p->smooth_width = 7;
+    p->damping = 0.9f;
+    p->step = 0.5f;
+    p->keep_state = 0;
+    return FR_OK;
+}
+
+int fr_params_parse_ini(const char* text, fr_params* p) {
+    g_parse_error.clear();
+    if (!text || !p) {
+        g_parse_error = "NULL argument";
+        return FR_ERR_INVALID_ARG;
+    }
+    std::istringstream in(text);
+    std::string line;
+    int lineno = 0;
+    while (std::getline(in, line)) {
+        ++lineno;
+        size_t hash = line.find('#');
+        if (hash != std::string::npos) line = line.substr(0, hash);
+        line = trim(line);
+        if (line.empty()) continue;
+        if (line.front() == '[' && line.back() == ']') continue;  // section headers are ignored
+        size_t eq = line.find('=');
+        if (eq == std::string::npos) {
+            g_parse_error = "line " + std::to_string(lineno) + ": expected KEY=VALUE";
+            return FR_ERR_PARSE;
+        }
+        std::string why;
+        int rc = set_key(p, trim(line.substr(0, eq)), trim(line.substr(eq + 1)), &why);
+        if (rc != FR_OK) {
+            g_parse_error = "line " + std::to_string(lineno) + ": " + why;
+            return rc;
+        }
+    }
+    return FR_OK;
+}
+
+int fr_params_load_ini(const char* path, fr_params* p) {
+    g_parse_error.clear();
+    if (!path || !p) {
+        g_parse_error = "NULL argument";
+        return FR_ERR_INVALID_ARG;
+    }
+    std::ifstream f(path);
+    if (!f) {
+        g_parse_error = std::string("cannot open ") + path;
+        return FR_ERR_IO;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    return fr_params_parse_ini(ss.str().c_str(), p);
+}
+
+int fr_create(const fr_params* p, fr_handle** out) {
+    if (!out) return FR_ERR_INVALID_ARG;
+    *out = nullptr;
+    fr_handle* h = new (std::nothrow) fr_handle();
+    if (!h) return FR_ERR_ALLOC;
+    int rc = check_params(h, p);
+    if (rc != FR_OK) {
+        g_parse_error = h->err;
+        delete h;
+        return rc;
+    }
+    h->P = *p;
+    if (cudaGetDevice(&h->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+        cudaGetLastError();
+        g_parse_error = "no CUDA device available";
+        delete h;
+        return FR_ERR_CUDA;
+    }
+    *out = h;
+    return FR_OK;
+}
+
+int fr_destroy(fr_handle* h) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    cudaDeviceSynchronize();
+    release(h);
+    if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+    delete h;
+    return FR_OK;
+}
+
+int fr_begin(fr_handle* h, const fr_pair* pairs, int n_pairs, void* stream) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    return begin(h, pairs, n_pairs, (cudaStream_t)stream);
+}
+
+int fr_step(fr_handle* h, int iter, float t, void* stream) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    if (!h->have_state) return fail(h, FR_ERR_STATE, "fr_step before fr_begin");
+    if (iter < 1 || iter > h->trace_cap) return fail(h, FR_ERR_INVALID_ARG, "iter %d outside [1, %d]", iter, h->trace_cap);
+    if (!(t > 0.f)) return fail(h, FR_ERR_INVALID_ARG, "t must be > 0");
+    int rc = launch_iter(h, iter, t, (cudaStream_t)stream);
+    if (rc == FR_OK) {
+        h->last_iter = iter;
+        h->stats_ready = false;
+        h->last_stream = (cudaStream_t)stream;
+    }
+    return rc;
+}
+
+int fr_finish(fr_handle* h, void* stream) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    if (!h->have_state) return fail(h, FR_ERR_STATE, "fr_finish before fr_begin");
+    return finish(h, (cudaStream_t)stream);
+}
+
+int fr_register_batch(fr_handle* h, const fr_pair* pairs, int n_pairs, void* stream) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = begin(h, pairs, n_pairs, s);
+    if (rc != FR_OK) return rc;
+    rc = run_registration(h, s);
+    if (rc != FR_OK && rc != FR_ERR_NUMERIC) return rc;
+    int rc2 = finish(h, s);
+    if (rc2 != FR_OK) return rc2;
+    if (h->P.verbosity > 0) {
+        int rc3 = host_stats(h);
+        if (rc3 != FR_OK) return rc3;
+        for (int p = 0; p < h->npairs; ++p) {
+            const fr_stats& st = h->stats[p];
+            printf("POST-REGISTRATION\nDICE COEFFICIENT\n");
+            for (int l = 1; l < h->P.no_labels; ++l) printf("label %d: %g\n", l, st.dice[l]);
+            printf("all labels: %g\n", st.dice_all);
+        }
+    }
+    return rc;
+}
+
+int fr_register(fr_handle* h, float* img_T, int16_t* lab_T, float* img_S, int16_t* lab_S, void* stream) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    fr_pair pr;
+    pr.dims[0] = h->P.volume_dims[0];
+    pr.dims[1] = h->P.volume_dims[1];
+    pr.dims[2] = h->P.volume_dims[2];
+    pr.img_T = img_T;
+    pr.lab_T = lab_T;
+    pr.img_S = img_S;
+    pr.lab_S = lab_S;
+    return fr_register_batch(h, &pr, 1, stream);
+}
+
+int fr_get_stats(fr_handle* h, int pair, fr_stats* out) {
+    if (!h || !out) return FR_ERR_INVALID_ARG;
+    if (!h->finished) return fail(h, FR_ERR_STATE, "no finished registration");
+    if (pair < 0 || pair >= h->npairs) return fail(h, FR_ERR_INVALID_ARG, "pair %d outside [0, %d)", pair, h->npairs);
+    int rc = host_stats(h);
+    if (rc != FR_OK) return rc;
+    *out = h->stats[pair];
+    return FR_OK;
+}
+
+int fr_get_trace(fr_handle* h, int pair, float* norms, int64_t* voxels, int cap, int* n_out) {
+    if (!h || cap < 0) return FR_ERR_INVALID_ARG;
+    if (!h->have_state) return fail(h, FR_ERR_STATE, "no registration");
+    if (pair < 0 || pair >= h->npairs) return fail(h, FR_ERR_INVALID_ARG, "pair %d outside [0, %d)", pair, h->npairs);
+    FR_CUDA(h, cudaStreamSynchronize(h->last_stream));
+    int stop = 0;
+    FR_CUDA(h, cudaMemcpy(&stop, h->stop + pair, sizeof(int), cudaMemcpyDeviceToHost));
+    const int n = stop ? stop : h->last_iter;
+    std::vector<unsigned long long> tr((size_t)h->npairs * h->trace_cap);
+    FR_CUDA(h, cudaMemcpy(tr.data(), h->trace, sizeof(unsigned long long) * tr.size(), cudaMemcpyDeviceToHost));
+    const int m = std::min(n, cap);
+    for (int i = 0; i < m; ++i) {
+        unsigned long long k = tr[(size_t)i * h->npairs + pair];
+        unsigned bits = (unsigned)(k >> 32);
+        if (norms) std::memcpy(norms + i, &bits, 4);
+        if (voxels) voxels[i] = bits ? (int64_t)(0xffffffffu - (unsigned)(k & 0xffffffffu)) : 0;
+    }
+    if (n_out) *n_out = n;
+    return FR_OK;
+}
+
+static int field_ptrs(fr_handle* h, int pair, int which, float** bufs, int* ncomp, int* nbufs) {
+    if (!h->have_state) return fail(h, FR_ERR_STATE, "no registration state");
+    if (pair < 0 || pair >= h->npairs) return fail(h, FR_ERR_INVALID_ARG, "pair %d outside [0, %d)", pair, h->npairs);
+    const bool ref = h->P.solver == FR_SOLVER_REFERENCE;
+    switch (which) {
+        case FR_FIELD_PSI:
+            bufs[0] = h->psi;
+            *ncomp = 3;
+            *nbufs = 1;
+            return FR_OK;
+        case FR_FIELD_PSI_INV:
+            if (!ref) return fail(h, FR_ERR_INVALID_ARG, "the sobolev solver keeps no psi_inv");
+            bufs[0] = h->pinv[0];
+            bufs[1] = h->pinv[1];
+            *ncomp = 3;
+            *nbufs = 2;
+            return FR_OK;
+        case FR_FIELD_V:
+            bufs[0] = h->v[0];
+            bufs[1] = h->v[1];
+            *ncomp = 3;
+            *nbufs = ref ? 2 : 1;
+            return FR_OK;
+        case FR_FIELD_RHO:
+            if (!ref) return fail(h, FR_ERR_INVALID_ARG, "the sobolev solver keeps no density");
+            bufs[0] = h->rho[0];
+            bufs[1] = h->rho[1];
+            *ncomp = 1;
+            *nbufs = 2;
+            return FR_OK;
+        default:
+            return fail(h, FR_ERR_INVALID_ARG, "unknown field %d", which);
+    }
+}
+
+int fr_get_field(fr_handle* h, int pair, int which, float* d_buf, void* stream) {
+    if (!h || !d_buf) return FR_ERR_INVALID_ARG;
+    float* bufs[2] = {nullptr, nullptr};
+    int ncomp = 0, nbufs = 0;
+    int rc = field_ptrs(h, pair, which, bufs, &ncomp, &nbufs);
+    if (rc != FR_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int sel = 0;
+    if (nbufs == 2) {
+        FR_CUDA(h, cudaStreamSynchronize(h->last_stream));
+        int stop = 0;
+        FR_CUDA(h, cudaMemcpy(&stop, h->stop + pair, sizeof(int), cudaMemcpyDeviceToHost));
+        sel = (stop ? stop : h->last_iter) & 1;
+    }
+    const Pair& P = h->hpairs[pair];
+    for (int c = 0; c < ncomp; ++c)
+        FR_CUDA(h, cudaMemcpyAsync(d_buf + c * P.N, bufs[sel] + c * h->NT + P.off, sizeof(float) * P.N,
+                                   cudaMemcpyDeviceToDevice, s));
+    return FR_OK;
+}
+
+int fr_set_field(fr_handle* h, int pair, int which, const float* d_buf, void* stream) {
+    if (!h || !d_buf) return FR_ERR_INVALID_ARG;
+    float* bufs[2] = {nullptr, nullptr};
+    int ncomp = 0, nbufs = 0;
+    int rc = field_ptrs(h, pair, which, bufs, &ncomp, &nbufs);
+    if (rc != FR_OK) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    const Pair& P = h->hpairs[pair];
+    for (int b = 0; b < nbufs; ++b)
+        for (int c = 0; c < ncomp; ++c)
+            FR_CUDA(h, cudaMemcpyAsync(bufs[b] + c * h->NT + P.off, d_buf + c * P.N, sizeof(float) * P.N,
+                                       cudaMemcpyDeviceToDevice, s));
+    h->stats_ready = false;
+    return FR_OK;
+}
+
+int fr_time_kernels(fr_handle* h, int iters, float* ms, int* n_kernels, void* stream) {
+    if (!h || !ms || iters < 1) return FR_ERR_INVALID_ARG;
+    if (!h->have_state) return fail(h, FR_ERR_STATE, "fr_time_kernels before fr_begin");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int nk = kernels_per_iter(h);
+    cudaEvent_t ev[6];
+    for (int k = 0; k <= nk; ++k) FR_CUDA(h, cudaEventCreate(&ev[k]));
+    std::vector<double> acc(nk, 0.0);
+    std::vector<float> ts = t_schedule(h->P);
+    int rc = FR_OK;
+    for (int it = 1; it <= iters && rc == FR_OK; ++it) {
+        // iterations cycle through the schedule; every kernel reads what it would read
+        const int slot = 1 + (it - 1) % std::max(h->trace_cap, 1);
+        const float t = ts.empty() ? h->P.alpha : ts[(slot - 1) % ts.size()];
+        rc = launch_iter(h, slot, t, s, ev);
+        if (rc != FR_OK) break;
+        FR_CUDA(h, cudaEventSynchronize(ev[nk]));
+        for (int k = 0; k < nk; ++k) {
+            float m = 0.f;
+            FR_CUDA(h, cudaEventElapsedTime(&m, ev[k], ev[k + 1]));
+            acc[k] += m;
+        }
+        h->last_iter = slot;
+    }
+    for (int k = 0; k <= nk; ++k) cudaEventDestroy(ev[k]);
+    if (rc != FR_OK) return rc;
+    for (int k = 0; k < nk; ++k) ms[k] = (float)(acc[k] / iters);
+    if (n_kernels) *n_kernels = nk;
+    h->stats_ready = false;
+    return FR_OK;
+}
+
+int fr_warp(const float* d_pos, const float* d_img, const int16_t* d_lab, const int dims[3], float* d_out,
+            int16_t* d_out_lab, void* stream) {
+    g_parse_error.clear();
+    if (!d_pos || !d_img || !d_out || !dims) {
+        g_parse_error = "fr_warp: NULL argument";
+        return FR_ERR_INVALID_ARG;
+    }
+    if (d_out_lab && !d_lab) {
+        g_parse_error = "fr_warp: d_out_lab given without d_lab";
+        return FR_ERR_INVALID_ARG;
+    }
+    if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) {
+        g_parse_error = "fr_warp: dims must be >= 1";
+        return FR_ERR_INVALID_ARG;
+    }
+    Pair P{};
+    P.X = dims[0];
+    P.Y = dims[1];
+    P.Z = dims[2];
+    P.N = (long long)P.X * P.Y * P.Z;
+    P.off = 0;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)frg::warp_kernel, 256, 0);
+    long long want = (P.N + 255) / 256;
+    int grid = (int)std::max(1LL, std::min<long long>(want, (long long)std::max(per_sm, 1) * std::max(sms, 1)));
+    frg::warp_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_pos, d_img, d_lab, d_out, d_out_lab, P);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_parse_error = std::string("fr_warp: ") + cudaGetErrorString(e);
+        return FR_ERR_CUDA;
+    }
+    return FR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,146 @@
+// fr_common.cuh -- shared device-side types and helpers of the fastreg GB300 kernels.
+//
+// Layout in HBM (all pairs of a cohort packed into one allocation per field):
+//   scalar field  f[off_p + i]                    i = x + X*(y + Y*z), x fastest
+//   vector field  f[c*NT + off_p + i], c = 0,1,2  three planes (SoA), NT = packed voxels
+// off_p is the voxel offset of pair p, rounded up to 32 voxels (128 B) so that every
+// x-row of every pair starts a coalesced segment when X is a multiple of 32.
+//
+// Arithmetic contract (mirrored by the CPU oracle): the library is compiled with
+// --fmad=false, so a*b+c is never contracted; the only fused multiply-adds are the
+// explicit fmaf() calls of lerp (include/cuda/cuda_utils.hpp:43-46 of the reference).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace frg {
+
+// One registration pair inside a packed cohort.
+struct Pair {
+    int X, Y, Z, pad;
+    long long off;  // voxel offset into the packed arrays
+    long long N;    // X*Y*Z
+};
+
+// A tile of work: pair index and the tile origin (x0, y0, z0).
+typedef int4 Tile;
+
+constexpr int kTileX = 32;  // threads along x (one warp per row)
+constexpr int kTileY = 8;   // rows per block
+constexpr int kTileZ = 8;   // slices marched by each thread
+
+__device__ __forceinline__ long long lin(const Pair& P, int x, int y, int z) {
+    return (long long)x + (long long)P.X * ((long long)y + (long long)P.Y * z);
+}
+
+// lerp(v0, v1, t) = fma(t, v0, fma(-t, v1, v1))
+__device__ __forceinline__ float lerpf_(float v0, float v1, float t) { return fmaf(t, v0, fmaf(-t, v1, v1)); }
+
+// Sample cell: clamp to [0, dim-1], floor corner, fractional weights
+// (interpolate_intensity / interpolate_field, include/cuda/cuda_utils.hpp:60-136).
+struct Cell {
+    long long base;  // linear index of the floor corner
+    int gx, gy, gz;
+    float a, b, c;
+};
+
+__device__ __forceinline__ Cell locate(const Pair& P, float px, float py, float pz) {
+    Cell cl;
+    float cx = fminf(fmaxf(0.f, px), (float)(P.X - 1));
+    float cy = fminf(fmaxf(0.f, py), (float)(P.Y - 1));
+    float cz = fminf(fmaxf(0.f, pz), (float)(P.Z - 1));
+    cl.gx = (int)floorf(cx);
+    cl.gy = (int)floorf(cy);
+    cl.gz = (int)floorf(cz);
+    cl.a = cx - (float)cl.gx;
+    cl.b = cy - (float)cl.gy;
+    cl.c = cz - (float)cl.gz;
+    cl.base = lin(P, cl.gx, cl.gy, cl.gz);
+    return cl;
+}
+
+// Trilinear sample with the unchecked corner addressing of the reference's
+// Volume/VectorField operator(): the +1 corner of a cell on the upper face aliases
+// to the next row/slice (weight 0 there); an index past the last voxel is clamped.
+// F points at the pair's plane (already offset by off_p).
+__device__ __forceinline__ float tri_unchecked(const float* __restrict__ F, const Pair& P, const Cell& cl) {
+    const long long X = P.X, XY = (long long)P.X * P.Y, last = P.N - 1;
+    const long long b = cl.base;
+    auto at = [&](long long d) -> float {
+        long long j = b + d;
+        return __ldg(F + (j < last ? j : last));
+    };
+    float f111 = at(1 + X + XY), f110 = at(1 + X), f101 = at(1 + XY), f100 = at(1);
+    float f011 = at(X + XY), f010 = at(X), f001 = at(XY), f000 = __ldg(F + b);
+    return lerpf_(lerpf_(lerpf_(f111, f110, cl.c), lerpf_(f101, f100, cl.c), cl.b),
+                  lerpf_(lerpf_(f011, f010, cl.c), lerpf_(f001, f000, cl.c), cl.b), cl.a);
+}
+
+// Trilinear sample with get_global_idx addressing (include/cuda/cuda_utils.hpp:31-37,
+// 109-136): a corner outside the grid reads element 0 of the field.
+__device__ __forceinline__ float tri_checked(const float* __restrict__ F, const Pair& P, const Cell& cl) {
+    const long long X = P.X, XY = (long long)P.X * P.Y;
+    const long long b = cl.base;
+    const bool ox = cl.gx + 1 < P.X, oy = cl.gy + 1 < P.Y, oz = cl.gz + 1 < P.Z;
+    const float f0 = __ldg(F);
+    float f000 = __ldg(F + b);
+    float f100 = ox ? __ldg(F + b + 1) : f0;
+    float f010 = oy ? __ldg(F + b + X) : f0;
+    float f001 = oz ? __ldg(F + b + XY) : f0;
+    float f110 = (ox && oy) ? __ldg(F + b + 1 + X) : f0;
+    float f101 = (ox && oz) ? __ldg(F + b + 1 + XY) : f0;
+    float f011 = (oy && oz) ? __ldg(F + b + X + XY) : f0;
+    float f111 = (ox && oy && oz) ? __ldg(F + b + 1 + X + XY) : f0;
+    return lerpf_(lerpf_(lerpf_(f111, f110, cl.c), lerpf_(f101, f100, cl.c), cl.b),
+                  lerpf_(lerpf_(f011, f010, cl.c), lerpf_(f001, f000, cl.c), cl.b), cl.a);
+}
+
+// sqrt rounded toward -inf (reference norm(), include/cuda/cuda_utils.hpp:251-253)
+__device__ __forceinline__ float norm3_rd(float x, float y, float z) {
+    return __fsqrt_rd((x * x + y * y) + z * z);
+}
+
+// (norm, index) packed so that a larger key means a larger norm and, for equal
+// norms, a lower linear index.  norm >= 0, so its IEEE bits order like the value.
+__device__ __forceinline__ unsigned long long norm_key(float nrm, long long idx) {
+    return ((unsigned long long)__float_as_uint(nrm) << 32) | (unsigned long long)(0xffffffffu - (unsigned)idx);
+}
+
+// Block-wide max of a 64-bit key; every thread must call it.  Returns the block max
+// in thread 0.
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long k, unsigned long long* smem) {
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long other = __shfl_xor_sync(0xffffffffu, k, o);
+        k = other > k ? other : k;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) smem[warp] = k;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        k = lane < nw ? smem[lane] : 0ull;
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long other = __shfl_xor_sync(0xffffffffu, k, o);
+            k = other > k ? other : k;
+        }
+    }
+    __syncthreads();
+    return k;
+}
+
+__device__ __forceinline__ double block_sum_f64(double v, double* smem) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) smem[warp] = v;
+    __syncthreads();
+    const int nw = blockDim.x >> 5;
+    if (warp == 0) {
+        v = lane < nw ? smem[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    __syncthreads();
+    return v;
+}
+
+}  // namespace frg

@@ -1,0 +1,100 @@
+// fr_kernels.h -- kernel argument blocks and launch entry points shared between the
+// kernel translation units and the C-ABI implementation (fr_api.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "fr_common.cuh"
+
+namespace frg {
+
+// Arguments of one reference-mode iteration (all three launches take the same block).
+struct RefIterArgs {
+    const Pair* pairs;
+    const Tile* tiles;
+    int ntiles;
+    int npairs;
+    long long NT;  // packed voxels (plane stride of vector fields)
+
+    const float* S;  // source intensities (packed)
+    const float* T;  // target intensities (packed)
+
+    const float* rho;   // density, read
+    const float* v;     // velocity, read
+    const float* pinv;  // psi_inv, read
+    float* rho_n;       // density, written
+    float* v_n;         // velocity, written
+    float* pinv_n;      // psi_inv, written
+    float* psi;         // psi (in place)
+    float* L;           // -Laplacian(psi) scratch
+
+    float alpha, f1, m2, tau, w_reg, max_update_norm;
+    int iter;        // 1-based iteration number
+    int first_iter;  // T o psi_inv is T itself on the first iteration of a call
+
+    int* stop;                 // per pair: iteration at which it converged (0 = running)
+    unsigned long long* keys;  // per pair: max-norm key of the running iteration
+    unsigned long long* trace; // [max_iter][npairs] max-norm keys
+    unsigned int* counter;     // last-block ticket of pass B
+};
+
+__global__ void ref_laplacian_kernel(RefIterArgs a);
+__global__ void ref_pass_a_kernel(RefIterArgs a);
+__global__ void ref_pass_b_kernel(RefIterArgs a);
+
+// Caller-owned buffers of one pair (device pointers); outputs overwrite inputs in place
+// exactly like FastReg::operator() (src/fastreg/fastreg.cpp:58-75).
+struct PairIO {
+    float* img_T;
+    int16_t* lab_T;
+    float* img_S;
+    int16_t* lab_S;
+};
+
+// Arguments of the start-of-registration and end-of-registration kernels.
+struct IoArgs {
+    const Pair* pairs;
+    const Tile* tiles;
+    int ntiles;
+    int npairs;
+    long long NT;
+    const PairIO* io;
+
+    float* S;
+    float* T;
+    int16_t* labS;
+    int16_t* labT;
+    float* rho0;
+    float* rho1;
+    float* v0;
+    float* v1;
+    float* psi;
+    float* pinv0;
+    float* pinv1;
+    float rho_init;
+    int keep_state;
+    int sobolev;        // sobolev solver: no rho/psi_inv, nearest-neighbour labels
+    int write_outputs;  // 0: statistics only (verbose energy)
+
+    // final stage
+    const int* stop;    // per pair convergence iteration (0 = ran max_iter)
+    int max_iter;
+    int no_labels;
+    double* tile_partials;      // [ntiles][2]: e_data, e_reg
+    long long* tile_folds;      // [ntiles]
+    unsigned long long* dice;   // [npairs][2*256 + 1]: inter, count, out of range
+    double* pair_energy;        // [npairs][2]
+    long long* pair_folds;      // [npairs]
+    unsigned int* counter;
+};
+
+__global__ void pack_init_kernel(IoArgs a);
+__global__ void finalize_kernel(IoArgs a);
+
+// Standalone trilinear warp of one volume (a1 of the hot path).
+__global__ void warp_kernel(const float* __restrict__ pos, const float* __restrict__ img,
+                            const int16_t* __restrict__ lab, float* __restrict__ out,
+                            int16_t* __restrict__ out_lab, Pair P);
+
+}  // namespace frg

@@ -1,0 +1,61 @@
+// fr_sob.h -- the sobolev solver: SSD data term, Gaussian-smoothed (Sobolev) gradient,
+// heavy-ball momentum and a compositional update of the deformation.
+//
+// One iteration, per voxel x of every pair (phi = positions, m = momentum):
+//   W(x)   = S(phi(x))                         trilinear, cell floor clamped to dim-2
+//   g(x)   = (W(x) - T(x)) * dW/dphi(x)        exact derivative of the trilinear
+//                                              interpolant (0 along a clamped axis)
+//   gs     = G_sigma * g                       separable Gaussian, SMOOTH_WIDTH taps,
+//                                              normalised, replicate boundary
+//   m      = DAMPING * m - STEP * gs
+//   phi(x) = phi(x) + m(phi(x))                trilinear gather of the new m
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fr_common.cuh"
+
+namespace frg {
+
+constexpr int kMaxSmoothWidth = 15;
+constexpr int kSobTileY = 8;
+constexpr int kSobTileZ = 8;
+// the start/end kernels walk sobolev tiles with the reference tile extents
+static_assert(kSobTileY == kTileY && kSobTileZ == kTileZ, "tile extents must agree");
+
+struct SobIterArgs {
+    const Pair* pairs;
+    const Tile* tiles;
+    int ntiles;
+    int npairs;
+    long long NT;
+    const float* S;
+    const float* T;
+    float* phi;   // positions (3 planes)
+    float* m;     // momentum (3 planes)
+    float* g;     // gradient (3 planes)
+    float* tmp;   // smoothing temporary (3 planes)
+    float damping, step;
+    float taps[kMaxSmoothWidth];
+    int radius;
+    float max_update_norm;
+    int iter;
+    int* stop;
+    unsigned long long* keys;
+    unsigned long long* trace;
+    double* energy;  // [max_iter][npairs] 0.5 * sum (W - T)^2 before the update
+    unsigned int* counter;
+};
+
+// Gaussian taps exp(-k^2 / (2 sigma^2)), k = -R..R, normalised; computed in double
+// and rounded to float.
+void gaussian_taps(float sigma, int width, float* taps);
+
+__global__ void sob_grad_kernel(SobIterArgs a);
+__global__ void sob_smooth_kernel(SobIterArgs a, int axis, const float* src, float* dst, int momentum);
+__global__ void sob_pass_b_kernel(SobIterArgs a);
+
+// grids: {grad, smooth, pass_b}; with `ev` (6 events) each launch is bracketed
+cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t s, cudaEvent_t* ev = nullptr);
+
+}  // namespace frg

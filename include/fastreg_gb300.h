@@ -1,0 +1,157 @@
+/*
+ * fastreg_gb300.h -- C ABI of the GB300-native fastreg registration loop.
+ *
+ * Plain C: pointers, sizes and status codes only.  Every call returns an int
+ * status (FR_OK = 0) and never exits the process; fr_last_error() gives the
+ * message of the last failure on a handle.  Device pointers are CUDA device
+ * pointers of the current device; `stream` is a cudaStream_t passed as void*
+ * (NULL = the legacy default stream).
+ *
+ * Each entry point names the reference interface it replaces (paths are inside
+ * the fastreg source tree).
+ */
+#ifndef FASTREG_GB300_H
+#define FASTREG_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FR_ABI_VERSION 1
+
+/* status codes */
+#define FR_OK 0
+#define FR_ERR_INVALID_ARG 1 /* bad pointer, size or parameter value */
+#define FR_ERR_CUDA 2        /* a CUDA runtime call or kernel launch failed */
+#define FR_ERR_ALLOC 3       /* device or host allocation failed */
+#define FR_ERR_IO 4          /* a file could not be opened or read */
+#define FR_ERR_PARSE 5       /* a params.ini line could not be parsed */
+#define FR_ERR_STATE 6       /* call out of order (e.g. stats before a registration) */
+#define FR_ERR_NUMERIC 7     /* the solver produced NaN/Inf */
+
+/* solver selection (params.ini key SOLVER=) */
+#define FR_SOLVER_REFERENCE 0 /* the reference's accelerated PDE flow */
+#define FR_SOLVER_SOBOLEV 1   /* SSD + Gaussian-smoothed gradient + momentum */
+
+/* fields for fr_get_field / fr_set_field */
+#define FR_FIELD_PSI 0     /* psi, 3 planes of positions (voxel units) */
+#define FR_FIELD_PSI_INV 1 /* psi_inv, 3 planes */
+#define FR_FIELD_V 2       /* velocity, 3 planes (sobolev: momentum) */
+#define FR_FIELD_RHO 3     /* density, 1 plane (reference solver only) */
+
+#define FR_MAX_LABELS 256
+
+/* Solver parameters: struct Params (include/params.hpp:7-26) plus the keys of the
+ * sobolev solver.  Field names follow the params.ini keys. */
+typedef struct fr_params {
+    int volume_dims[3];    /* VOL_DIMS_X/Y/Z */
+    float volume_size[3];  /* VOL_SIZE_X/Y/Z (parsed, unused by the solver, as in the reference) */
+    int no_labels;         /* NO_LABELS (<= FR_MAX_LABELS) */
+    int max_iter;          /* MAX_ITER */
+    float max_update_norm; /* MAX_UPDATE_NORM */
+    float rho_0;           /* RHO_0 */
+    float tau;             /* TAU */
+    float w_reg;           /* W_REG */
+    float alpha;           /* ALPHA */
+    float p;               /* p */
+    float C;               /* C */
+    int reset_iter;        /* RESET_ITER (<= 0: never) */
+    int verbosity;         /* 0, 1 (--verbose), 2 (--vverbose) */
+    /* additions (new params.ini keys) */
+    int solver;            /* SOLVER=reference|sobolev */
+    float smooth_sigma;    /* SMOOTH_SIGMA (sobolev) */
+    int smooth_width;      /* SMOOTH_WIDTH, odd, <= 15 (sobolev) */
+    float damping;         /* DAMPING (sobolev momentum) */
+    float step;            /* STEP (sobolev step size) */
+    int keep_state;        /* KEEP_STATE=1: continue from the previous call's fields,
+                              as FastReg::operator() does on a reused instance */
+} fr_params;
+
+typedef struct fr_handle fr_handle;
+
+/* One pair of a cohort: caller-owned device buffers, overwritten in place
+ * (img_T/lab_T <- T o psi_inv, img_S/lab_S <- S o psi; fastreg.cpp:71-72). */
+typedef struct fr_pair {
+    int dims[3];
+    float *img_T;
+    int16_t *lab_T;
+    float *img_S;
+    int16_t *lab_S;
+} fr_pair;
+
+/* Results of the last registration of one pair. */
+typedef struct fr_stats {
+    int iterations;            /* iterations run */
+    int converged;             /* 1 if MAX_UPDATE_NORM stopped the solver */
+    float last_max_update_norm;
+    int64_t last_max_update_voxel; /* linear index x + X*(y + Y*z) */
+    double e_data;             /* 0.5 * sum (T - S o psi)^2, FP64 */
+    double e_reg;              /* 0.5 * sum ||J_u||_F^2, FP64 */
+    double energy;             /* e_data + w_reg * e_reg */
+    int64_t folds;             /* #{voxels : det(I + J_u) <= 0} */
+    int no_labels;
+    double dice[FR_MAX_LABELS]; /* per label 2|A n B| / (|A| + |B|) (NaN if both empty) */
+    double dice_all;           /* pooled over labels 1..no_labels-1 */
+    int64_t dice_out_of_range; /* voxels whose label is outside [0, no_labels) */
+    int64_t dice_inter[FR_MAX_LABELS];
+    int64_t dice_count[FR_MAX_LABELS];
+} fr_stats;
+
+/* ---- parameters: Params + the app's Boost parse of params.ini (demo.cpp:96-149) ---- */
+int fr_params_default(fr_params *p);
+int fr_params_parse_ini(const char *text, fr_params *p); /* text of a params.ini */
+int fr_params_load_ini(const char *path, fr_params *p);
+
+/* ---- solver lifetime: FastReg(const Params&) (fastreg.hpp:14, fastreg.cpp:24-46)
+ *      and Solver(Params&) (solver.hpp:64-66, solver.cpp:7-65) ---- */
+int fr_create(const fr_params *p, fr_handle **out);
+int fr_destroy(fr_handle *h);
+
+/* ---- one registration: FastReg::operator() (fastreg.hpp:24, fastreg.cpp:58-75) ->
+ *      Solver::estimate_psi (solver.hpp:68-78) -> device::estimate_psi (solver.cu:295-444).
+ *      Enqueued on `stream`; outputs are ready when the stream reaches them. ---- */
+int fr_register(fr_handle *h, float *img_T, int16_t *lab_T, float *img_S, int16_t *lab_S, void *stream);
+
+/* ---- a cohort of independent pairs of uneven sizes in one set of launches per
+ *      iteration (no counterpart in the reference, which runs one pair per process) ---- */
+int fr_register_batch(fr_handle *h, const fr_pair *pairs, int n_pairs, void *stream);
+
+/* ---- results: the reference prints them (solver.cu:40-47,408-424, reductor.cpp:357-360) ---- */
+int fr_get_stats(fr_handle *h, int pair, fr_stats *out);
+int fr_get_trace(fr_handle *h, int pair, float *norms, int64_t *voxels, int cap, int *n_out);
+
+/* ---- fields of the last registration: FastReg::getDeformationField() (fastreg.hpp:22).
+ *      d_buf holds 3*N floats for vector fields, N for rho. ---- */
+int fr_get_field(fr_handle *h, int pair, int which, float *d_buf, void *stream);
+int fr_set_field(fr_handle *h, int pair, int which, const float *d_buf, void *stream);
+
+/* ---- the phases of one registration, for callers that step the solver themselves
+ *      (the reference's estimate_psi loop body, solver.cu:329-433) ---- */
+int fr_begin(fr_handle *h, const fr_pair *pairs, int n_pairs, void *stream); /* pack + init */
+int fr_step(fr_handle *h, int iter, float t, void *stream);                 /* one iteration */
+int fr_finish(fr_handle *h, void *stream);                                  /* outputs + stats */
+
+/* ---- measurement: run `iters` iterations from the current state with CUDA events
+ *      around every launch on `stream`; ms[k] = mean duration of kernel k of one
+ *      iteration (reference solver: k = 0 Laplacian, 1 pass A, 2 pass B; sobolev:
+ *      0 gradient, 1 smoothing x, 2 smoothing y, 3 smoothing z + momentum, 4 pass B);
+ *      n_kernels receives the count.  No counterpart in the reference. ---- */
+int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *stream);
+
+/* ---- standalone kernels of the hot path ---- */
+/* apply (vector_fields.cu:81-107): out = img o pos (trilinear), out_lab = lab at the floor
+ * corner; pos is 3 planes of N positions; d_lab/d_out_lab may be NULL. */
+int fr_warp(const float *d_pos, const float *d_img, const int16_t *d_lab, const int dims[3], float *d_out,
+            int16_t *d_out_lab, void *stream);
+
+const char *fr_last_error(const fr_handle *h);
+const char *fr_status_string(int status);
+int fr_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTREG_GB300_H */

@@ -1,0 +1,72 @@
+"""Batched cohorts and the sobolev solver on the GPU against the CPU oracle."""
+import numpy as np
+import pytest
+
+from fastreg_gb300 import FastReg, Params, _native as N
+from oracle import oracle as O
+from tests.helpers import assert_bitexact, images, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _to(dev, a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+@pytest.mark.parametrize("solver", ["reference", "sobolev"])
+def test_batch_equals_pairs_alone(cuda, solver):
+    """A cohort of uneven pairs in one set of launches gives, pair by pair, the bits
+    of each pair registered alone (and of the oracle)."""
+    dims_list = [(20, 18, 16), (33, 17, 21), (16, 24, 12), (40, 9, 10)]
+    kw = dict(no_labels=4, max_iter=25, alpha=0.02, solver=solver, step=0.5, damping=0.9)
+    pairs_np = [images(d, 50 + k) for k, d in enumerate(dims_list)]
+    P = Params(volume_dims=dims_list[0], **kw)
+    fr = FastReg(P)
+    bufs = [tuple(_to(cuda, p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+    fr.register_batch(bufs)
+    for k, (d, p) in enumerate(zip(dims_list, pairs_np)):
+        psi_b = fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy()
+        Pk = Params(volume_dims=d, **kw)
+        if solver == "reference":
+            o = O.ref_register(Pk, p["T"], p["labT"], p["S"], p["labS"])
+            assert_bitexact(psi_b, o["psi"], f"pair {k} psi")
+            assert_bitexact(bufs[k][2].cpu().numpy(), o["out_S"], f"pair {k} S o psi")
+            assert_bitexact(bufs[k][3].cpu().numpy(), o["out_labS"], f"pair {k} labels")
+            assert_bitexact(bufs[k][0].cpu().numpy(), o["out_T"], f"pair {k} T o psi_inv")
+        else:
+            o = O.sob_register(Pk, p["T"], p["S"])
+            assert_bitexact(psi_b, o["phi"], f"pair {k} phi")
+            w = O.warp(o["phi"], p["S"])
+            assert_bitexact(bufs[k][2].cpu().numpy(), w, f"pair {k} S o phi")
+            lab = O.warp_nearest_label(o["phi"], p["labS"])
+            assert_bitexact(bufs[k][3].cpu().numpy(), lab, f"pair {k} nearest labels")
+        st = fr.stats(pair=k)
+        assert st.iterations == 25
+
+
+@pytest.mark.parametrize("dims", [(12, 10, 9), (33, 17, 20)])
+def test_sobolev_registration(cuda, dims):
+    d = images(dims, 11 + dims[0])
+    P = Params(volume_dims=dims, no_labels=4, max_iter=30, solver="sobolev", smooth_sigma=1.5, smooth_width=7,
+               damping=0.9, step=0.5)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    phi = fr.get_field(N.FR_FIELD_PSI).cpu().numpy()
+    m = fr.get_field(N.FR_FIELD_V).cpu().numpy()
+    o = O.sob_register(P, d["T"], d["S"])
+    assert_bitexact(phi, o["phi"], "phi")
+    assert_bitexact(m, o["m"], "momentum")
+    norms, vox = fr.trace()
+    assert_bitexact(norms, o["trace_norm"], "update norms")
+    assert_bitexact(vox, o["trace_idx"], "update voxels")
+    # targets are left as they are by the sobolev solver
+    assert_bitexact(iT.cpu().numpy(), d["T"], "T unchanged")
+    st = fr.stats()
+    W = O.warp(o["phi"], d["S"])
+    e = 0.5 * float(((d["T"].astype(np.float64) - W.astype(np.float64)) ** 2).sum())
+    assert rel_err(st.e_data, e) < 1e-12
+    o64 = O.sob_register(P, d["T"], d["S"], prec=64)
+    err = np.abs(phi - o64["phi"]).max()
+    assert err < 1e-3, f"phi vs FP64 oracle: max abs err {err} voxels"

@@ -1,0 +1,171 @@
+"""Reference-mode parity on the GPU: the CUDA path through the C ABI against the
+CPU oracle (fr_oracle.c, op-order matched), bit for bit."""
+import numpy as np
+import pytest
+
+from fastreg_gb300 import FastReg, Params, _native as N
+from oracle import oracle as O
+from tests.helpers import assert_bitexact, images, random_state, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _to(dev, a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def _params(dims, **kw):
+    base = dict(volume_dims=dims, no_labels=4, max_iter=8, alpha=0.05, tau=0.2, w_reg=0.2, rho_0=1.0, p=2.0, C=0.25,
+                reset_iter=-1, max_update_norm=-1e-10)
+    base.update(kw)
+    return Params(**base)
+
+
+@pytest.mark.parametrize("dims", [(7, 9, 11), (33, 17, 20), (40, 36, 30)])
+@pytest.mark.parametrize("iter_no", [1, 2, 7])
+def test_one_iteration_from_random_state(cuda, dims, iter_no):
+    """One iteration (L, pass A, pass B) from a random mid-registration state."""
+    seed = 10 * dims[0] + iter_no
+    d = images(dims, seed)
+    st = random_state(dims, seed + 1, disp=1.5, vel=0.3)
+    P = _params(dims)
+    fr = FastReg(P)
+    tens = [_to(cuda, d[k]) for k in ("T", "labT", "S", "labS")]
+    fr.begin([tuple(tens)])
+    fr.set_field(N.FR_FIELD_RHO, _to(cuda, st["rho"]))
+    fr.set_field(N.FR_FIELD_V, _to(cuda, st["v"]))
+    fr.set_field(N.FR_FIELD_PSI, _to(cuda, st["psi"]))
+    fr.set_field(N.FR_FIELD_PSI_INV, _to(cuda, st["psi_inv"]))
+    t = P.alpha * iter_no
+    fr.step(iter_no, t)
+    rho_g = fr.get_field(N.FR_FIELD_RHO).cpu().numpy()
+    v_g = fr.get_field(N.FR_FIELD_V).cpu().numpy()
+    psi_g = fr.get_field(N.FR_FIELD_PSI).cpu().numpy()
+    pinv_g = fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy()
+    norms, vox = fr.trace()
+
+    k = O.ref_coef(P.alpha, np.float32(t), P.p, P.C, P.tau, P.w_reg)
+    L = O.ref_laplacian(st["psi"])
+    rho_o, v_o, pinv_o = O.ref_pass_a(k, d["S"], d["T"], iter_no == 1, st["rho"], st["v"], st["psi_inv"], L)
+    psi_o, mx, am = O.ref_pass_b(P.alpha, v_o, st["psi"])
+
+    assert_bitexact(rho_g, rho_o, "rho")
+    assert_bitexact(v_g, v_o, "v")
+    assert_bitexact(pinv_g, pinv_o, "psi_inv")
+    assert_bitexact(psi_g, psi_o, "psi")
+    assert np.float32(norms[iter_no - 1]) == np.float32(mx)
+    assert int(vox[iter_no - 1]) == am
+    fr.close()
+
+
+@pytest.mark.parametrize("dims,iters", [((12, 10, 9), 30), ((24, 20, 18), 60), ((64, 64, 64), 200)])
+def test_full_registration(cuda, dims, iters):
+    """A whole registration through FastReg::operator() semantics (in place)."""
+    import torch
+    d = images(dims, 7 + dims[0])
+    P = _params(dims, max_iter=iters, alpha=0.02)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    assert fr(iT, lT, iS, lS)
+    st = fr.stats()
+    psi_g = fr.get_field(N.FR_FIELD_PSI).cpu().numpy()
+    pinv_g = fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy()
+    norms, vox = fr.trace()
+
+    o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    assert st.iterations == o["iterations"] == iters
+    assert_bitexact(psi_g, o["psi"], "psi")
+    assert_bitexact(pinv_g, o["psi_inv"], "psi_inv")
+    assert_bitexact(iT.cpu().numpy(), o["out_T"], "T o psi_inv")
+    assert_bitexact(iS.cpu().numpy(), o["out_S"], "S o psi")
+    assert_bitexact(lT.cpu().numpy(), o["out_labT"], "labels T o psi_inv")
+    assert_bitexact(lS.cpu().numpy(), o["out_labS"], "labels S o psi")
+    assert_bitexact(norms, o["trace_norm"], "max update norms")
+    assert_bitexact(vox, o["trace_idx"], "max update voxels")
+
+    os_ = O.stats(d["T"], d["labT"], o["out_S"], o["out_labS"], o["psi"], P.no_labels)
+    assert rel_err(st.e_data, os_["e_data"]) < 1e-12
+    assert rel_err(st.e_reg, os_["e_reg"]) < 1e-12
+    assert st.folds == os_["folds"]
+    assert st.dice_inter == list(os_["dice_inter"][:P.no_labels])
+    assert st.dice_count == list(os_["dice_count"][:P.no_labels])
+    assert st.dice_out_of_range == os_["dice_out_of_range"]
+    # the FP64 oracle agrees with the FP32 path to the stated tolerance
+    o64 = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"], prec=64)
+    err = rel_err(psi_g, o64["psi"]).max()
+    assert err < 1e-5, f"psi vs FP64 oracle: max rel err {err}"
+    fr.close()
+
+
+def test_warp_standalone(cuda):
+    """fr_warp (apply_kernel) on random positions, including positions outside the
+    grid and NaN, against the oracle: intensities and floor-corner labels bit-exact."""
+    import torch
+    from fastreg_gb300 import warp
+    r = np.random.Generator(np.random.PCG64(5))
+    for dims in [(7, 9, 11), (33, 17, 20), (64, 64, 64)]:
+        X, Y, Z = dims
+        img = r.normal(0, 1, (Z, Y, X)).astype(np.float32)
+        lab = r.integers(0, 8, (Z, Y, X)).astype(np.int16)
+        pos = np.stack([r.uniform(-2, X + 1, (Z, Y, X)), r.uniform(-2, Y + 1, (Z, Y, X)),
+                        r.uniform(-2, Z + 1, (Z, Y, X))]).astype(np.float32)
+        pos[:, 0, 0, :3] = np.nan
+        pos[0, 1, 1, 1] = X - 1  # exactly on the upper face
+        out, out_lab = warp(_to(cuda, pos), _to(cuda, img), _to(cuda, lab))
+        o_img, o_lab = O.warp(pos, img, lab)
+        assert_bitexact(out.cpu().numpy(), o_img, f"warp {dims}")
+        assert_bitexact(out_lab.cpu().numpy(), o_lab, f"warp labels {dims}")
+
+
+def test_convergence_stops_on_device(cuda):
+    """MAX_UPDATE_NORM reached -> the solver stops at that iteration, on the device
+    (graph path), with the same state as the oracle's break (solver.cu:418-421)."""
+    dims = (24, 20, 18)
+    d = images(dims, 99)
+    P0 = _params(dims, max_iter=40, alpha=0.02)
+    o_full = O.ref_register(P0, d["T"], d["labT"], d["S"], d["labS"])
+    thr = float(np.float32(o_full["trace_norm"][12]))  # stop where the norm first drops to this
+    P = _params(dims, max_iter=40, alpha=0.02, max_update_norm=thr)
+    o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    assert o["converged"] and o["iterations"] < 40
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    st = fr.stats()
+    assert st.converged and st.iterations == o["iterations"]
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi"], "psi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy(), o["psi_inv"], "psi_inv")
+    assert_bitexact(iS.cpu().numpy(), o["out_S"], "S o psi")
+    assert_bitexact(iT.cpu().numpy(), o["out_T"], "T o psi_inv")
+
+
+def test_reset_iter_schedule(cuda):
+    """RESET_ITER restarts t (solver.cu:428-432)."""
+    dims = (16, 14, 12)
+    d = images(dims, 3)
+    P = _params(dims, max_iter=25, alpha=0.03, reset_iter=7)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi"], "psi")
+    assert_bitexact(iS.cpu().numpy(), o["out_S"], "S o psi")
+
+
+def test_keep_state_carries_fields_over(cuda):
+    """KEEP_STATE=1 continues from the previous call's psi/psi_inv/v like a reused
+    FastReg instance (fastreg.cpp:58-75 never clears the solver)."""
+    dims = (16, 14, 12)
+    d = images(dims, 4)
+    P = _params(dims, max_iter=9, alpha=0.03, keep_state=1)
+    fr = FastReg(P)
+    bufs = [_to(cuda, d[k]) for k in ("T", "labT", "S", "labS")]
+    fr(*bufs)
+    bufs = [_to(cuda, d[k]) for k in ("T", "labT", "S", "labS")]
+    fr(*bufs)
+    o1 = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    state = dict(rho=o1["rho"], v=o1["v"], psi=o1["psi"], psi_inv=o1["psi_inv"])
+    o2 = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"], state=state)
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o2["psi"], "psi after 2 calls")
+    assert_bitexact(bufs[2].cpu().numpy(), o2["out_S"], "S o psi after 2 calls")
