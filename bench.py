@@ -198,6 +198,27 @@ def run_reference_arm(args):
     return 0
 
 
+def profile_case(args):
+    """The bench workload, launched once, for ncu captures."""
+    import torch
+    from fastreg_gb300 import FastReg, synthetic as sy, warp, _native as N
+    dev = torch.device("cuda", 0)
+    data = sy.make_pair(sy.CFG2)
+    P = reference_params(DIMS, args.iters, solver=args.solver)
+    fr = FastReg(P)
+    bufs = [torch.from_numpy(data[k]).to(dev) for k in ("T", "labT", "S", "labS")]
+    fr(*bufs)
+    psi = fr.get_field(N.FR_FIELD_PSI)
+    img = torch.from_numpy(data["S"]).to(dev)
+    lab = torch.from_numpy(data["labS"]).to(dev)
+    warp(psi, img, lab)
+    torch.cuda.synchronize()
+    st = fr.stats()
+    print(f"profile case: {args.solver} solver, {st.iterations} iterations, e_data {st.e_data:.6g}")
+    fr.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -205,8 +226,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-extras", action="store_true", help="skip the sobolev/warp/kernel/CPU measurements")
-    ap.add_argument("--profile", action="store_true", help="short run for an ncu launch list")
+    ap.add_argument("--profile", action="store_true",
+                    help="one registration of the bench pair with --iters iterations and one standalone warp, "
+                         "for ncu (no timing, no JSON line)")
+    ap.add_argument("--iters", type=int, default=ITERS, help="iterations of the --profile registration")
+    ap.add_argument("--solver", default="reference", choices=["reference", "sobolev"],
+                    help="solver of the --profile registration")
     args = ap.parse_args()
+    if args.profile:
+        return profile_case(args)
     if args.warmup < 3 and not args.profile:
         args.warmup = 3
 

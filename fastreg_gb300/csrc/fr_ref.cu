@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256) ref_pass_b_kernel(RefIterArgs a) {
         unsigned long long best = 0ull;
         if (x >= 1 && x <= P.X - 2 && y >= 1 && y <= P.Y - 2) {
             const long long NT = a.NT;
-            const float* __restrict__ v = a.v + P.off;
+            const float* __restrict__ v = a.v_n + P.off;  // the velocity pass A just wrote
             float* psi = a.psi + P.off;
             const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
             for (int z = z0; z < z1; ++z) {

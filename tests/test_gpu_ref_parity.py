@@ -91,10 +91,12 @@ def test_full_registration(cuda, dims, iters):
     assert st.dice_inter == list(os_["dice_inter"][:P.no_labels])
     assert st.dice_count == list(os_["dice_count"][:P.no_labels])
     assert st.dice_out_of_range == os_["dice_out_of_range"]
-    # the FP64 oracle agrees with the FP32 path to the stated tolerance
+    # FP32 rounding drift against the FP64 oracle, in voxels (positions are O(dims),
+    # so a relative bound on them would say little about the displacement)
     o64 = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"], prec=64)
-    err = rel_err(psi_g, o64["psi"]).max()
-    assert err < 1e-5, f"psi vs FP64 oracle: max rel err {err}"
+    err = float(np.abs(psi_g.astype(np.float64) - o64["psi"]).max())
+    err_inv = float(np.abs(pinv_g.astype(np.float64) - o64["psi_inv"]).max())
+    assert err < 1e-3 and err_inv < 1e-3, f"FP32 vs FP64 drift: psi {err}, psi_inv {err_inv} voxels"
     fr.close()
 
 
