@@ -96,6 +96,65 @@ __device__ __forceinline__ float tri_checked(const float* __restrict__ F, const 
                   lerpf_(lerpf_(f011, f010, cl.c), lerpf_(f001, f000, cl.c), cl.b), cl.a);
 }
 
+// ---- 32-bit variants used inside one pair (N < 2^31) ----
+
+struct Cell32 {
+    int base;  // linear index of the floor corner inside the pair
+    int gx, gy, gz;
+    float a, b, c;
+};
+
+__device__ __forceinline__ Cell32 locate32(int X, int Y, int Z, float px, float py, float pz) {
+    Cell32 cl;
+    const float cx = fminf(fmaxf(0.f, px), (float)(X - 1));
+    const float cy = fminf(fmaxf(0.f, py), (float)(Y - 1));
+    const float cz = fminf(fmaxf(0.f, pz), (float)(Z - 1));
+    cl.gx = (int)floorf(cx);
+    cl.gy = (int)floorf(cy);
+    cl.gz = (int)floorf(cz);
+    cl.a = cx - (float)cl.gx;
+    cl.b = cy - (float)cl.gy;
+    cl.c = cz - (float)cl.gz;
+    cl.base = cl.gx + X * (cl.gy + Y * cl.gz);
+    return cl;
+}
+
+__device__ __forceinline__ float trilerp(float f111, float f110, float f101, float f100, float f011, float f010,
+                                         float f001, float f000, float a, float b, float c) {
+    return lerpf_(lerpf_(lerpf_(f111, f110, c), lerpf_(f101, f100, c), b),
+                  lerpf_(lerpf_(f011, f010, c), lerpf_(f001, f000, c), b), a);
+}
+
+// tri_unchecked with 32-bit indices: corners past the last voxel (only possible when
+// the cell touches the end of the array) are clamped on a slow path.
+__device__ __forceinline__ float tri_unchecked32(const float* __restrict__ F, int X, int XY, int N, const Cell32& cl) {
+    const int b = cl.base;
+    if (b + 1 + X + XY <= N - 1) {
+        return trilerp(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), __ldg(F + b + 1 + XY), __ldg(F + b + 1),
+                       __ldg(F + b + X + XY), __ldg(F + b + X), __ldg(F + b + XY), __ldg(F + b), cl.a, cl.b, cl.c);
+    }
+    const int last = N - 1;
+    return trilerp(__ldg(F + min(b + 1 + X + XY, last)), __ldg(F + min(b + 1 + X, last)),
+                   __ldg(F + min(b + 1 + XY, last)), __ldg(F + min(b + 1, last)), __ldg(F + min(b + X + XY, last)),
+                   __ldg(F + min(b + X, last)), __ldg(F + min(b + XY, last)), __ldg(F + b), cl.a, cl.b, cl.c);
+}
+
+// tri_checked with 32-bit indices: corners outside the grid read element 0.
+__device__ __forceinline__ float tri_checked32(const float* __restrict__ F, int X, int Y, int Z, int XY,
+                                               const Cell32& cl) {
+    const int b = cl.base;
+    const bool ox = cl.gx + 1 < X, oy = cl.gy + 1 < Y, oz = cl.gz + 1 < Z;
+    if (ox && oy && oz) {
+        return trilerp(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), __ldg(F + b + 1 + XY), __ldg(F + b + 1),
+                       __ldg(F + b + X + XY), __ldg(F + b + X), __ldg(F + b + XY), __ldg(F + b), cl.a, cl.b, cl.c);
+    }
+    const float f0 = __ldg(F);
+    return trilerp((ox && oy && oz) ? __ldg(F + b + 1 + X + XY) : f0, (ox && oy) ? __ldg(F + b + 1 + X) : f0,
+                   (ox && oz) ? __ldg(F + b + 1 + XY) : f0, ox ? __ldg(F + b + 1) : f0,
+                   (oy && oz) ? __ldg(F + b + X + XY) : f0, oy ? __ldg(F + b + X) : f0, oz ? __ldg(F + b + XY) : f0,
+                   __ldg(F + b), cl.a, cl.b, cl.c);
+}
+
 // sqrt rounded toward -inf (reference norm(), include/cuda/cuda_utils.hpp:251-253)
 __device__ __forceinline__ float norm3_rd(float x, float y, float z) {
     return __fsqrt_rd((x * x + y * y) + z * z);

@@ -29,13 +29,14 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         if (x < 1 || x > P.X - 2 || y < 1 || y > P.Y - 2) continue;
-        const long long X = P.X, XY = (long long)P.X * P.Y;
+        const int X = P.X, XY = P.X * P.Y;
         const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
-        for (int z = z0; z < z1; ++z) {
-            const long long i = P.off + lin(P, x, y, z);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float* __restrict__ Q = a.psi + c * a.NT;
+        for (int c = 0; c < 3; ++c) {
+            const float* __restrict__ Q = a.psi + c * a.NT + P.off;
+            float* Lc = a.L + c * a.NT + P.off;
+            for (int z = z0; z < z1; ++z) {
+                const int i = x + X * y + XY * z;
                 float s = -6.f * __ldg(Q + i);
                 s = s + __ldg(Q + i + 1);
                 s = s + __ldg(Q + i - 1);
@@ -43,7 +44,7 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
                 s = s + __ldg(Q + i - X);
                 s = s + __ldg(Q + i + XY);
                 s = s + __ldg(Q + i - XY);
-                a.L[c * a.NT + i] = -1.f * s;
+                Lc[i] = -1.f * s;
             }
         }
     }
@@ -56,132 +57,137 @@ __device__ __forceinline__ float det_ref(const float m[3][3]) {
     return first - second;
 }
 
+// entropy flux of the (Dv)v diagonal term (vector_fields.cu:376-378)
+__device__ __forceinline__ float entropy_flux(float c, float n) {
+    return ((fmaxf(c, 0.f) * fmaxf(c, 0.f) - fminf(c, 0.f) * fminf(c, 0.f)) + fminf(n, 0.f) * fminf(n, 0.f)) -
+           fmaxf(n, 0.f) * fmaxf(n, 0.f);
+}
+
 // ----------------------------------------------------------------------------------
 // fused pass A
 // ----------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) ref_pass_a_kernel(RefIterArgs a) {
+__global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const Tile tl = a.tiles[t];
         if (a.stop[tl.x]) continue;
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         if (x < 1 || x > P.X - 2 || y < 1 || y > P.Y - 2) continue;
-        const long long X = P.X, XY = (long long)P.X * P.Y, NT = a.NT;
+        const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y, N = (int)P.N;
+        const long long NT = a.NT;
         const float* __restrict__ S = a.S + P.off;
         const float* __restrict__ T = a.T + P.off;
         const float* __restrict__ rho = a.rho + P.off;
-        const float* __restrict__ vx_ = a.v + P.off;
-        const float* __restrict__ vy_ = vx_ + NT;
-        const float* __restrict__ vz_ = vy_ + NT;
-        const float* __restrict__ pinv = a.pinv + P.off;
-        const float* __restrict__ L = a.L + P.off;
-        const bool dv_y = y >= 2 && y <= P.Y - 2;
-        const bool dv_x = x >= 2 && x <= P.X - 3;
-        const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
+        const float* __restrict__ V[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
+        const float* __restrict__ Q[3] = {a.pinv + P.off, a.pinv + NT + P.off, a.pinv + 2 * NT + P.off};
+        const float* __restrict__ Lp[3] = {a.L + P.off, a.L + NT + P.off, a.L + 2 * NT + P.off};
+        float* rho_n = a.rho_n + P.off;
+        float* Vn[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
+        float* Qn[3] = {a.pinv_n + P.off, a.pinv_n + NT + P.off, a.pinv_n + 2 * NT + P.off};
+        const bool dv_xy = x >= 2 && x <= X - 3 && y >= 2 && y <= Y - 2;
+        const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, Z - 1);
         for (int z = z0; z < z1; ++z) {
-            const long long i = lin(P, x, y, z);
+            const int i = x + X * y + XY * z;
 
-            // divergence of rho*v (upwind) and the density update
-            const float vx = __ldg(vx_ + i), vy = __ldg(vy_ + i), vz = __ldg(vz_ + i);
-            const float p = __ldg(rho + i);
-            const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * __ldg(rho + i + 1);
-            const float vxm = __ldg(vx_ + i - 1);
-            const float t12 = (vxm > 0.f) ? vxm * __ldg(rho + i - 1) : vxm * p;
-            const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * __ldg(rho + i + X);
-            const float vym = __ldg(vy_ + i - X);
-            const float t22 = (vym > 0.f) ? vym * __ldg(rho + i - X) : vym * p;
-            const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * __ldg(rho + i + XY);
-            const float vzm = __ldg(vz_ + i - XY);
-            const float t32 = (vzm > 0.f) ? vzm * __ldg(rho + i - XY) : vzm * p;
-            const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
-            const float rho_new = p + a.alpha * div;
-            a.rho_n[P.off + i] = rho_new;
+            // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
+            const float q[3] = {__ldg(Q[0] + i), __ldg(Q[1] + i), __ldg(Q[2] + i)};
+            const Cell32 cl = locate32(X, Y, Z, q[0], q[1], q[2]);
+            const float Tq = a.first_iter ? __ldg(T + i) : tri_unchecked32(T, X, XY, N, cl);
+            float Lq[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) Lq[c] = tri_unchecked32(Lp[c], X, XY, N, cl);
 
-            // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z)
+            // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
             float M[3][3];
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
-                const float* __restrict__ Q = pinv + r * NT;
-                M[r][0] = (__ldg(Q + i + 1) - __ldg(Q + i - 1)) * 0.5f;
-                M[r][1] = (__ldg(Q + i + X) - __ldg(Q + i - X)) * 0.5f;
-                M[r][2] = (__ldg(Q + i + XY) - __ldg(Q + i - XY)) * 0.5f;
+                M[r][0] = (__ldg(Q[r] + i + 1) - __ldg(Q[r] + i - 1)) * 0.5f;
+                M[r][1] = (__ldg(Q[r] + i + X) - __ldg(Q[r] + i - X)) * 0.5f;
+                M[r][2] = (__ldg(Q[r] + i + XY) - __ldg(Q[r] + i - XY)) * 0.5f;
             }
             const float det = det_ref(M);
 
-            // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
-            const Cell cl = locate(P, __ldg(pinv + i), __ldg(pinv + NT + i), __ldg(pinv + 2 * NT + i));
-            const float Tq = a.first_iter ? __ldg(T + i) : tri_unchecked(T, P, cl);
-            float Lq[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) Lq[c] = tri_unchecked(L + c * NT, P, cl);
-
             // central-difference gradient of S and the potential gradient
-            float gs[3];
-            gs[0] = (__ldg(S + i + 1) - __ldg(S + i - 1)) * 0.5f;
-            gs[1] = (__ldg(S + i + X) - __ldg(S + i - X)) * 0.5f;
-            gs[2] = (__ldg(S + i + XY) - __ldg(S + i - XY)) * 0.5f;
-            const float diff = __ldg(S + i) - Tq;
+            const float Si = __ldg(S + i);
+            const float gs[3] = {(__ldg(S + i + 1) - __ldg(S + i - 1)) * 0.5f,
+                                 (__ldg(S + i + X) - __ldg(S + i - X)) * 0.5f,
+                                 (__ldg(S + i + XY) - __ldg(S + i - XY)) * 0.5f};
+            const float diff = Si - Tq;
             float gU[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (a.w_reg * Lq[c])) * det;
 
-            // (Dv)v
-            const float vxp_x = __ldg(vx_ + i + 1), vyp_y = __ldg(vy_ + i + X), vzp_z = __ldg(vz_ + i + XY);
-            const float ax1 = ((fmaxf(vx, 0.f) * fmaxf(vx, 0.f) - fminf(vx, 0.f) * fminf(vx, 0.f)) +
-                               fminf(vxp_x, 0.f) * fminf(vxp_x, 0.f)) -
-                              fmaxf(vxp_x, 0.f) * fmaxf(vxp_x, 0.f);
-            const float ax2 = (vy > 0.f) ? vy * (vx - __ldg(vx_ + i - X)) : vy * (__ldg(vx_ + i + X) - vx);
-            const float ax3 = (vz > 0.f) ? vz * (vx - __ldg(vx_ + i - XY)) : vz * (__ldg(vx_ + i + XY) - vx);
-            const float ay1 = (vx > 0.f) ? vx * (vy - __ldg(vy_ + i - 1)) : vx * (__ldg(vy_ + i + 1) - vy);
-            const float ay2 = ((fmaxf(vy, 0.f) * fmaxf(vy, 0.f) - fminf(vy, 0.f) * fminf(vy, 0.f)) +
-                               fminf(vyp_y, 0.f) * fminf(vyp_y, 0.f)) -
-                              fmaxf(vyp_y, 0.f) * fmaxf(vyp_y, 0.f);
-            const float ay3 = (vz > 0.f) ? vz * (vy - __ldg(vy_ + i - XY)) : vz * (__ldg(vy_ + i + XY) - vy);
-            const float az1 = (vx > 0.f) ? vx * (vz - __ldg(vz_ + i - 1)) : vx * (__ldg(vz_ + i + 1) - vz);
-            const float az2 = (vy > 0.f) ? vy * (vz - __ldg(vz_ + i - X)) : vy * (__ldg(vz_ + i + X) - vz);
-            const float az3 = ((fmaxf(vz, 0.f) * fmaxf(vz, 0.f) - fminf(vz, 0.f) * fminf(vz, 0.f)) +
-                               fminf(vzp_z, 0.f) * fminf(vzp_z, 0.f)) -
-                              fmaxf(vzp_z, 0.f) * fmaxf(vzp_z, 0.f);
-            float dvv[3];
-            dvv[0] = (0.5f * ax1 + ax2) + ax3;
-            dvv[1] = (ay1 + 0.5f * ay2) + ay3;
-            dvv[2] = (az1 + az2) + 0.5f * az3;
+            // velocity and its 6 neighbours, each loaded once
+            float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vc[c] = __ldg(V[c] + i);
+                vxm[c] = __ldg(V[c] + i - 1);
+                vxp[c] = __ldg(V[c] + i + 1);
+                vym[c] = __ldg(V[c] + i - X);
+                vyp[c] = __ldg(V[c] + i + X);
+                vzm[c] = __ldg(V[c] + i - XY);
+                vzp[c] = __ldg(V[c] + i + XY);
+            }
+            const float vx = vc[0], vy = vc[1], vz = vc[2];
+
+            // divergence of rho*v (upwind) and the density update
+            const float p = __ldg(rho + i);
+            const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * __ldg(rho + i + 1);
+            const float t12 = (vxm[0] > 0.f) ? vxm[0] * __ldg(rho + i - 1) : vxm[0] * p;
+            const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * __ldg(rho + i + X);
+            const float t22 = (vym[1] > 0.f) ? vym[1] * __ldg(rho + i - X) : vym[1] * p;
+            const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * __ldg(rho + i + XY);
+            const float t32 = (vzm[2] > 0.f) ? vzm[2] * __ldg(rho + i - XY) : vzm[2] * p;
+            const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
+            const float rho_new = p + a.alpha * div;
+            rho_n[i] = rho_new;
+
+            // (Dv)v: entropy scheme on the diagonal, upwind off the diagonal
+            const float ax1 = entropy_flux(vx, vxp[0]);
+            const float ax2 = (vy > 0.f) ? vy * (vx - vym[0]) : vy * (vyp[0] - vx);
+            const float ax3 = (vz > 0.f) ? vz * (vx - vzm[0]) : vz * (vzp[0] - vx);
+            const float ay1 = (vx > 0.f) ? vx * (vy - vxm[1]) : vx * (vxp[1] - vy);
+            const float ay2 = entropy_flux(vy, vyp[1]);
+            const float ay3 = (vz > 0.f) ? vz * (vy - vzm[1]) : vz * (vzp[1] - vy);
+            const float az1 = (vx > 0.f) ? vx * (vz - vxm[2]) : vx * (vxp[2] - vz);
+            const float az2 = (vy > 0.f) ? vy * (vz - vym[2]) : vy * (vyp[2] - vz);
+            const float az3 = entropy_flux(vz, vzp[2]);
+            const float dvv[3] = {(0.5f * ax1 + ax2) + ax3, (ay1 + 0.5f * ay2) + ay3, (az1 + az2) + 0.5f * az3};
 
             // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
             // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
             // reference does, and y+2 at y = Y-2 reads linear index i + 2X as is.
-            const float vel[3] = {vx, vy, vz};
             float dv[3] = {0.f, 0.f, 0.f};
-            if (dv_x && dv_y && z >= 2 && z <= P.Z - 3) {
+            if (dv_xy && z >= 2 && z <= Z - 3) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float* __restrict__ V = vx_ + c * NT;
-                    const float xx = (vx < 0.f) ? (__ldg(V + i + 2) - 2.f * __ldg(V + i + 1)) + vel[c]
-                                                : (vel[c] - 2.f * __ldg(V + i - 1)) + __ldg(V + i - 2);
-                    const float yy = (vy < 0.f) ? (__ldg(V + i + 2 * X) - 2.f * __ldg(V + i - X)) + vel[c]
-                                                : (vel[c] - 2.f * __ldg(V + i - X)) + __ldg(V + i - 2 * X);
-                    const float zz = (vz < 0.f) ? (__ldg(V + i + 2 * XY) - 2.f * __ldg(V + i - XY)) + vel[c]
-                                                : (vel[c] - 2.f * __ldg(V + i - XY)) + __ldg(V + i - 2 * XY);
+                    const float xx = (vx < 0.f) ? (__ldg(V[c] + i + 2) - 2.f * vxp[c]) + vc[c]
+                                                : (vc[c] - 2.f * vxm[c]) + __ldg(V[c] + i - 2);
+                    const float yy = (vy < 0.f) ? (__ldg(V[c] + i + 2 * X) - 2.f * vym[c]) + vc[c]
+                                                : (vc[c] - 2.f * vym[c]) + __ldg(V[c] + i - 2 * X);
+                    const float zz = (vz < 0.f) ? (__ldg(V[c] + i + 2 * XY) - 2.f * vzm[c]) + vc[c]
+                                                : (vc[c] - 2.f * vzm[c]) + __ldg(V[c] + i - 2 * XY);
                     dv[c] = -1.f * ((xx + yy) + zz);
                 }
             }
 
             // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
-            const float q = a.m2 / (fabsf(rho_new) + 1e-5f);
+            const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);
             float vn[3];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float friction = a.f1 * vel[c];
+                const float friction = a.f1 * vc[c];
                 const float diffusion = a.tau * dv[c];
-                const float potential = q * gU[c];
+                const float potential = qd * gU[c];
                 const float acc = ((friction + dvv[c]) - diffusion) + potential;
-                vn[c] = vel[c] - a.alpha * acc;
-                a.v_n[c * NT + P.off + i] = vn[c];
+                vn[c] = vc[c] - a.alpha * acc;
+                Vn[c][i] = vn[c];
             }
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 const float jv = ((M[r][0] * vn[0]) + (M[r][1] * vn[1])) + (M[r][2] * vn[2]);
-                a.pinv_n[r * NT + P.off + i] = __ldg(pinv + r * NT + i) - a.alpha * jv;
+                Qn[r][i] = q[r] - a.alpha * jv;
             }
         }
     }
@@ -201,20 +207,22 @@ __global__ void __launch_bounds__(256) ref_pass_b_kernel(RefIterArgs a) {
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         unsigned long long best = 0ull;
         if (x >= 1 && x <= P.X - 2 && y >= 1 && y <= P.Y - 2) {
+            const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y;
             const long long NT = a.NT;
-            const float* __restrict__ v = a.v_n + P.off;  // the velocity pass A just wrote
-            float* psi = a.psi + P.off;
+            // the velocity pass A just wrote
+            const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
+            float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
             const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
             for (int z = z0; z < z1; ++z) {
-                const long long i = lin(P, x, y, z);
-                const float px = psi[i], py = psi[NT + i], pz = psi[2 * NT + i];
-                const Cell cl = locate(P, px, py, pz);
-                const float ux = a.alpha * tri_checked(v, P, cl);
-                const float uy = a.alpha * tri_checked(v + NT, P, cl);
-                const float uz = a.alpha * tri_checked(v + 2 * NT, P, cl);
-                psi[i] = px + ux;
-                psi[NT + i] = py + uy;
-                psi[2 * NT + i] = pz + uz;
+                const int i = x + X * y + XY * z;
+                const float px = Q[0][i], py = Q[1][i], pz = Q[2][i];
+                const Cell32 cl = locate32(X, Y, Z, px, py, pz);
+                const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, XY, cl);
+                const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, XY, cl);
+                const float uz = a.alpha * tri_checked32(V[2], X, Y, Z, XY, cl);
+                Q[0][i] = px + ux;
+                Q[1][i] = py + uy;
+                Q[2][i] = pz + uz;
                 const float nrm = norm3_rd(ux, uy, uz);
                 if (nrm == nrm) {  // NaN norms never win, as in the reference's '>' test
                     const unsigned long long k = norm_key(nrm, i);

@@ -1,0 +1,61 @@
+"""ctypes front end of oracle/ref_runner.c (TEST INFRASTRUCTURE ONLY): runs the
+reference's own kernels (cubins built from the reference sources by
+oracle/ref_build.py) on the GPU, to produce golden outputs that pin the oracle."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REF_DIR = HERE / "_ref"
+
+
+class RRParams(C.Structure):
+    _fields_ = [("max_iter", C.c_int), ("reset_iter", C.c_int), ("max_update_norm", C.c_float),
+                ("rho_0", C.c_float), ("tau", C.c_float), ("w_reg", C.c_float), ("alpha", C.c_float),
+                ("p", C.c_float), ("C", C.c_float)]
+
+
+def available() -> bool:
+    return all((REF_DIR / f"{u}.cubin").exists() for u in ("solver", "vector_fields", "reductor", "scalar_fields",
+                                                            "volume"))
+
+
+def _lib():
+    path = REF_DIR / "libref_runner.so"
+    if not path.exists():
+        from oracle import ref_build
+        ref_build.build_runner()
+    lib = C.CDLL(str(path))
+    lib.rr_register.restype = C.c_int
+    lib.rr_last_error.restype = C.c_char_p
+    return lib
+
+
+def register(params, T, labT, S, labS):
+    """One registration with the reference kernels; params has the Params fields."""
+    lib = _lib()
+    T = np.ascontiguousarray(T, np.float32)
+    S = np.ascontiguousarray(S, np.float32)
+    labT = np.ascontiguousarray(labT, np.int16)
+    labS = np.ascontiguousarray(labS, np.int16)
+    z, y, x = T.shape
+    P = RRParams(int(params.max_iter), int(params.reset_iter), params.max_update_norm, params.rho_0, params.tau,
+                 params.w_reg, params.alpha, params.p, params.C)
+    dims = (C.c_int * 3)(x, y, z)
+    oT, oS = np.empty_like(T), np.empty_like(S)
+    olT, olS = np.empty_like(labT), np.empty_like(labS)
+    psi = np.empty((3, z, y, x), np.float32)
+    pinv = np.empty((3, z, y, x), np.float32)
+    n = max(int(params.max_iter), 1)
+    tn = np.zeros(n, np.float32)
+    ti = np.zeros(n, np.int64)
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    ran = lib.rr_register(str(REF_DIR).encode(), dims, C.byref(P), p(T), p(labT), p(S), p(labS), p(oT), p(olT),
+                          p(oS), p(olS), p(psi), p(pinv), p(tn), p(ti))
+    if ran < 0:
+        raise RuntimeError("reference run failed: " + lib.rr_last_error().decode())
+    return dict(out_T=oT, out_labT=olT, out_S=oS, out_labS=olS, psi=psi, psi_inv=pinv, iterations=int(ran),
+                trace_norm=tn[:ran], trace_idx=ti[:ran])
