@@ -132,3 +132,49 @@ def test_no_gpu_gives_a_status_not_an_exit():
     assert lib.fr_status_string(N.FR_ERR_CUDA) == b"CUDA error"
     dims = (C.c_int * 3)(8, 8, 8)
     assert lib.fr_warp(None, None, None, dims, None, None, None) == N.FR_ERR_INVALID_ARG
+
+
+CPP_CALLER = r'''
+#include <cstdio>
+#include "fastreg_compat.hpp"
+
+int main(int argc, char** argv) {
+    Params params = Params::from_ini(argv[1]);
+    std::printf("dims %d %d %d alpha %g iters %d\n", params.volume_dims[0], params.volume_dims[1],
+                params.volume_dims[2], params.alpha, params.max_iter);
+    try {
+        FastReg fastreg(params);
+        std::printf("created\n");
+    } catch (const fastreg_gb300::Error& e) {
+        std::printf("error %d\n", e.status);
+    }
+    return 0;
+}
+'''
+
+
+def test_cpp_shim_compiles_and_runs(tmp_path):
+    """A demo.cpp-style caller compiles against include/fastreg_compat.hpp (the
+    reference's Params/FastReg names) and runs; without a GPU, FastReg's
+    constructor throws fastreg_gb300::Error(FR_ERR_CUDA) instead of exiting."""
+    import shutil
+    import torch
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "caller.cpp"
+    src.write_text(CPP_CALLER)
+    ini = tmp_path / "params.ini"
+    ini.write_text(REFERENCE_INI)
+    exe = tmp_path / "caller"
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    cmd = ["g++", "-std=c++17", "-O1", str(src), "-o", str(exe), "-I", str(ROOT / "include"), "-I",
+           str(cuda / "include"), "-L", str(N.LIB_PATH.parent), "-lfastreg_gb300", "-L", str(cuda / "lib64"),
+           "-lcudart", f"-Wl,-rpath,{N.LIB_PATH.parent}", f"-Wl,-rpath,{cuda / 'lib64'}"]
+    subprocess.run(cmd, check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe), str(ini)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, out.stderr
+    assert "dims 193 229 193" in out.stdout and "iters 2048" in out.stdout
+    if not torch.cuda.is_available():
+        assert f"error {N.FR_ERR_CUDA}" in out.stdout
+    else:
+        assert "created" in out.stdout

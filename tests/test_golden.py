@@ -3,14 +3,15 @@
 The fixtures under tests/golden were produced by tests/golden/make_golden.py, which
 runs the reference's unmodified kernels (compiled from its sources, launched in its
 order by oracle/ref_runner.c) on a GB300.  The reference build uses --ftz=true,
---prec-div=false, --prec-sqrt=false and nvcc's default FMA contraction, so it is
-compared within tolerances, not bit for bit:
-  - positions psi / psi_inv: |oracle - reference| <= 1e-5 * max(1, |reference|);
-  - warped intensities: <= 1e-5 relative (floor 1e-6 absolute);
-  - max-update-norm trace: <= 1e-4 relative;
-  - floor-corner labels: identical wherever the sample position is farther than
-    1e-4 voxel from an integer grid plane (where the floor itself is decided by
-    the last bits of psi).
+--prec-div=false, --prec-sqrt=false and nvcc's default FMA contraction, which the
+oracle does not reproduce; on these cases the differences stay below the float
+resolution of the positions, and the check is:
+  - psi, psi_inv, T o psi_inv, S o psi and both warped label maps: bit for bit;
+  - the per-iteration max update norm (taken on the ~1e-5 voxel updates, where the
+    differences in the velocity do show): <= 1e-6 relative, same voxel.
+The looser bounds of the spec contract (1e-5 relative on float fields; labels
+equal away from integer grid planes) are asserted as well, so a failure says which
+bound broke.
 """
 from pathlib import Path
 
@@ -57,3 +58,10 @@ def test_oracle_matches_reference_kernels(path):
     for lab, pos in (("out_labS", o["psi"]), ("out_labT", o["psi_inv"])):
         diff = o[lab] != f[lab]
         assert not (diff & ~_near_grid(pos)).any(), f"{lab}: {int(diff.sum())} labels differ away from grid planes"
+    # observed: bit-exact
+    for k in ("psi", "psi_inv", "out_T", "out_S"):
+        assert np.array_equal(o[k].view(np.uint32), f[k].view(np.uint32)), f"{k} not bit-exact"
+    for k in ("out_labS", "out_labT"):
+        assert np.array_equal(o[k], f[k]), f"{k} not identical"
+    assert err.max() <= 1e-6
+    assert np.array_equal(o["trace_idx"], f["trace_idx"])

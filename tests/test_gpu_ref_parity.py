@@ -171,3 +171,33 @@ def test_keep_state_carries_fields_over(cuda):
     o2 = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"], state=state)
     assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o2["psi"], "psi after 2 calls")
     assert_bitexact(bufs[2].cpu().numpy(), o2["out_S"], "S o psi after 2 calls")
+
+
+GOLDEN = sorted((__import__("pathlib").Path(__file__).resolve().parent / "golden").glob("ref_*.npz"))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[p.stem for p in GOLDEN])
+def test_cuda_path_matches_reference_kernels(cuda, path):
+    """The CUDA path against the outputs of the reference's own CUDA kernels
+    (tests/golden, made by tests/golden/make_golden.py): bit for bit on psi,
+    psi_inv, the warped images and the warped labels."""
+    f = np.load(path)
+    dims = tuple(int(v) for v in f["dims"])
+    pv = f["params"]
+    P = Params(volume_dims=dims, no_labels=4, max_iter=int(pv[0]), reset_iter=int(pv[1]),
+               max_update_norm=float(pv[2]), rho_0=float(pv[3]), tau=float(pv[4]), w_reg=float(pv[5]),
+               alpha=float(pv[6]), p=float(pv[7]), C=float(pv[8]))
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, f[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    assert fr.stats().iterations == int(f["iterations"])
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), f["psi"], "psi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy(), f["psi_inv"], "psi_inv")
+    assert_bitexact(iT.cpu().numpy(), f["out_T"], "T o psi_inv")
+    assert_bitexact(iS.cpu().numpy(), f["out_S"], "S o psi")
+    assert_bitexact(lT.cpu().numpy(), f["out_labT"], "labels T o psi_inv")
+    assert_bitexact(lS.cpu().numpy(), f["out_labS"], "labels S o psi")
+    norms, vox = fr.trace()
+    assert np.abs(norms.astype(np.float64) - f["trace_norm"]).max() <= 1e-6 * float(np.abs(f["trace_norm"]).max())
+    assert_bitexact(vox, f["trace_idx"], "max update voxels")
+    fr.close()
