@@ -675,6 +675,10 @@ thread_local std::string g_parse_error;
 
 }  // namespace
 
+namespace frg {
+void set_global_error(const char* msg) { g_parse_error = msg ? msg : ""; }
+}  // namespace frg
+
 extern "C" {
 
 int fr_abi_version(void) { return FR_ABI_VERSION; }

@@ -146,6 +146,26 @@ int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *st
 int fr_warp(const float *d_pos, const float *d_img, const int16_t *d_lab, const int dims[3], float *d_out,
             int16_t *d_out_lab, void *stream);
 
+/* ---- statistics without device allocation ----
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc when they
+ * need the statistics of a registration (a process whose device memory belongs to
+ * another framework's pool, a real-time pipeline that forbids allocation after
+ * start-up): the same e_data / e_reg / energy / folds / Dice that fr_get_stats reports,
+ * computed from buffers the caller holds -- the original target d_T and its labels
+ * d_labT, the warped source d_warped_S / d_warped_labS (S o psi) and psi (3 planes of
+ * N positions) -- and written to the host struct *out (other fields zeroed).
+ * Its scratch is one file-scope __device__ array of FR_NOALLOC_SCRATCH_BYTES that every
+ * GPU loading this library keeps until exit; the function allocates nothing.  The
+ * first call on a device looks up that array's device address (make it before any
+ * stream capture).  Calls share the array: calls that overlap on the GPU race and must
+ * be serialised by the caller.  Limits: dims >= 2, N <= FR_NOALLOC_MAX_VOXELS,
+ * no_labels <= FR_MAX_LABELS; larger inputs return FR_ERR_INVALID_ARG with a message
+ * in fr_last_error(NULL).  The call synchronises `stream`. */
+#define FR_NOALLOC_SCRATCH_BYTES 28712
+#define FR_NOALLOC_MAX_VOXELS 2147483647LL
+int fr_stats_noalloc(const float *d_T, const int16_t *d_labT, const float *d_warped_S, const int16_t *d_warped_labS,
+                     const float *d_psi, const int dims[3], int no_labels, float w_reg, fr_stats *out, void *stream);
+
 const char *fr_last_error(const fr_handle *h);
 const char *fr_status_string(int status);
 int fr_abi_version(void);
