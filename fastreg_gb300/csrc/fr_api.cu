@@ -48,7 +48,8 @@ struct fr_handle {
     float *S = nullptr, *T = nullptr;
     int16_t *labS = nullptr, *labT = nullptr;
     float *rho[2] = {nullptr, nullptr}, *v[2] = {nullptr, nullptr}, *pinv[2] = {nullptr, nullptr};
-    float *psi = nullptr, *L = nullptr;
+    float* psi = nullptr;
+    float4* LT = nullptr;
     int* stop = nullptr;
     unsigned long long* keys = nullptr;
     unsigned long long* trace = nullptr;
@@ -149,9 +150,9 @@ int check_params(fr_handle* h, const fr_params* p) {
     return FR_OK;
 }
 
-int occupancy_grid(fr_handle* h, const void* fn, int ntiles) {
+int occupancy_grid(fr_handle* h, const void* fn, int ntiles, size_t smem = 0) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
     long long g = (long long)per_sm * h->num_sms;
     return (int)std::max(1LL, std::min<long long>(g, ntiles));
 }
@@ -231,9 +232,10 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         add((void**)&h->rho[1], sizeof(float) * NT);
         add((void**)&h->pinv[0], sizeof(float) * 3 * NT);
         add((void**)&h->pinv[1], sizeof(float) * 3 * NT);
-        add((void**)&h->L, sizeof(float) * 3 * NT);
+        add((void**)&h->LT, sizeof(float4) * NT);
     } else {
-        h->rho[0] = h->rho[1] = h->pinv[0] = h->pinv[1] = h->L = nullptr;
+        h->rho[0] = h->rho[1] = h->pinv[0] = h->pinv[1] = nullptr;
+        h->LT = nullptr;
         add((void**)&h->grad, sizeof(float) * 3 * NT);
         add((void**)&h->sob_energy, sizeof(double) * (size_t)n * want_trace);
     }
@@ -271,7 +273,10 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
 
     if (h->P.solver == FR_SOLVER_REFERENCE) {
         h->grid_lap = occupancy_grid(h, (const void*)frg::ref_laplacian_kernel, ntiles);
-        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, ntiles);
+        FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)frg::ref_pass_a_smem_bytes()));
+        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, ntiles, frg::ref_pass_a_smem_bytes());
         h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, ntiles);
     } else {
         h->grid_a = occupancy_grid(h, (const void*)frg::sob_grad_kernel, ntiles);
@@ -299,7 +304,7 @@ frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
     a.v_n = h->v[dst];
     a.pinv_n = h->pinv[dst];
     a.psi = h->psi;
-    a.L = h->L;
+    a.LT = h->LT;
     const fr_params& P = h->P;
     // solver.cu:198-199, evaluated once per iteration on the host in float
     const float m1 = P.p + 1.f;
@@ -323,7 +328,7 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
     if (ev) cudaEventRecord(ev[0], s);
     frg::ref_laplacian_kernel<<<h->grid_lap, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    frg::ref_pass_a_kernel<<<h->grid_a, 256, 0, s>>>(a);
+    frg::ref_pass_a_kernel<<<h->grid_a, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
     frg::ref_pass_b_kernel<<<h->grid_b, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);
@@ -384,6 +389,7 @@ frg::IoArgs io_args(fr_handle* h) {
     a.psi = h->psi;
     a.pinv0 = h->pinv[0];
     a.pinv1 = h->pinv[1];
+    a.LT = h->LT;
     a.rho_init = h->P.rho_0;
     a.keep_state = h->P.keep_state && h->have_state;
     a.sobolev = h->P.solver == FR_SOLVER_SOBOLEV;

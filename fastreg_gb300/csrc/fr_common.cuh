@@ -28,7 +28,7 @@ typedef int4 Tile;
 
 constexpr int kTileX = 32;  // threads along x (one warp per row)
 constexpr int kTileY = 8;   // rows per block
-constexpr int kTileZ = 8;   // slices marched by each thread
+constexpr int kTileZ = 16;  // slices marched by each thread
 
 __device__ __forceinline__ long long lin(const Pair& P, int x, int y, int z) {
     return (long long)x + (long long)P.X * ((long long)y + (long long)P.Y * z);
@@ -153,6 +153,43 @@ __device__ __forceinline__ float tri_checked32(const float* __restrict__ F, int 
                    (ox && oz) ? __ldg(F + b + 1 + XY) : f0, ox ? __ldg(F + b + 1) : f0,
                    (oy && oz) ? __ldg(F + b + X + XY) : f0, oy ? __ldg(F + b + X) : f0, oz ? __ldg(F + b + XY) : f0,
                    __ldg(F + b), cl.a, cl.b, cl.c);
+}
+
+__device__ __forceinline__ float4 lerp4_(float4 v0, float4 v1, float t) {
+    return make_float4(lerpf_(v0.x, v1.x, t), lerpf_(v0.y, v1.y, t), lerpf_(v0.z, v1.z, t), lerpf_(v0.w, v1.w, t));
+}
+
+// tri_unchecked32 on an interleaved 4-channel field (one 16-byte load per corner)
+__device__ __forceinline__ float4 tri_unchecked32_f4(const float4* __restrict__ F, int X, int XY, int N,
+                                                     const Cell32& cl) {
+    const int b = cl.base;
+    int o111 = b + 1 + X + XY, o110 = b + 1 + X, o101 = b + 1 + XY, o100 = b + 1;
+    int o011 = b + X + XY, o010 = b + X, o001 = b + XY;
+    if (o111 > N - 1) {
+        const int last = N - 1;
+        o111 = min(o111, last);
+        o110 = min(o110, last);
+        o101 = min(o101, last);
+        o100 = min(o100, last);
+        o011 = min(o011, last);
+        o010 = min(o010, last);
+        o001 = min(o001, last);
+    }
+    const float4 f111 = __ldg(F + o111), f110 = __ldg(F + o110), f101 = __ldg(F + o101), f100 = __ldg(F + o100);
+    const float4 f011 = __ldg(F + o011), f010 = __ldg(F + o010), f001 = __ldg(F + o001), f000 = __ldg(F + b);
+    return lerp4_(lerp4_(lerp4_(f111, f110, cl.c), lerp4_(f101, f100, cl.c), cl.b),
+                  lerp4_(lerp4_(f011, f010, cl.c), lerp4_(f001, f000, cl.c), cl.b), cl.a);
+}
+
+// ---- asynchronous global -> shared copies (cp.async, 4 bytes each) ----
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int Pending>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(Pending) : "memory");
 }
 
 // sqrt rounded toward -inf (reference norm(), include/cuda/cuda_utils.hpp:251-253)

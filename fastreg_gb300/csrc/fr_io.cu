@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(256) pack_init_kernel(IoArgs a) {
             }
             a.rho0[g] = a.rho_init;
             a.rho1[g] = a.rho_init;
+            a.LT[g] = make_float4(0.f, 0.f, 0.f, io.img_T[i]);  // the Laplacian is 0 on the boundary
             if (!a.keep_state) {
                 const float pos[3] = {(float)x, (float)y, (float)z};
 #pragma unroll

@@ -27,7 +27,7 @@ struct RefIterArgs {
     float* v_n;         // velocity, written
     float* pinv_n;      // psi_inv, written
     float* psi;         // psi (in place)
-    float* L;           // -Laplacian(psi) scratch
+    float4* LT;         // (-Laplacian(psi), T) interleaved: the two fields pass A gathers at psi_inv
 
     float alpha, f1, m2, tau, w_reg, max_update_norm;
     int iter;        // 1-based iteration number
@@ -40,6 +40,7 @@ struct RefIterArgs {
 };
 
 __global__ void ref_laplacian_kernel(RefIterArgs a);
+size_t ref_pass_a_smem_bytes();  // dynamic shared memory of ref_pass_a_kernel
 __global__ void ref_pass_a_kernel(RefIterArgs a);
 __global__ void ref_pass_b_kernel(RefIterArgs a);
 
@@ -72,6 +73,7 @@ struct IoArgs {
     float* psi;
     float* pinv0;
     float* pinv1;
+    float4* LT;
     float rho_init;
     int keep_state;
     int sobolev;        // sobolev solver: no rho/psi_inv, nearest-neighbour labels

@@ -20,7 +20,8 @@
 namespace frg {
 
 // ----------------------------------------------------------------------------------
-// L = -(sum of 6 neighbours - 6 psi), interior only
+// LT = (-(sum of 6 neighbours - 6 psi), T) on the interior; the boundary keeps the
+// (0, 0, 0, T) that pack_init_kernel wrote
 // ----------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
@@ -30,13 +31,18 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         if (x < 1 || x > P.X - 2 || y < 1 || y > P.Y - 2) continue;
         const int X = P.X, XY = P.X * P.Y;
+        const float* __restrict__ Q0 = a.psi + P.off;
+        const float* __restrict__ Q1 = Q0 + a.NT;
+        const float* __restrict__ Q2 = Q1 + a.NT;
+        const float* __restrict__ T = a.T + P.off;
+        float4* LT = a.LT + P.off;
         const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
+        for (int z = z0; z < z1; ++z) {
+            const int i = x + X * y + XY * z;
+            float l[3];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            const float* __restrict__ Q = a.psi + c * a.NT + P.off;
-            float* Lc = a.L + c * a.NT + P.off;
-            for (int z = z0; z < z1; ++z) {
-                const int i = x + X * y + XY * z;
+            for (int c = 0; c < 3; ++c) {
+                const float* __restrict__ Q = c == 0 ? Q0 : (c == 1 ? Q1 : Q2);
                 float s = -6.f * __ldg(Q + i);
                 s = s + __ldg(Q + i + 1);
                 s = s + __ldg(Q + i - 1);
@@ -44,8 +50,9 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
                 s = s + __ldg(Q + i - X);
                 s = s + __ldg(Q + i + XY);
                 s = s + __ldg(Q + i - XY);
-                Lc[i] = -1.f * s;
+                l[c] = -1.f * s;
             }
+            LT[i] = make_float4(l[0], l[1], l[2], __ldg(T + i));
         }
     }
 }
@@ -65,138 +72,255 @@ __device__ __forceinline__ float entropy_flux(float c, float n) {
 
 // ----------------------------------------------------------------------------------
 // fused pass A
+//
+// A block owns a 32 x 8 column tile and marches z.  The stencil operands (v with a
+// 2-voxel halo and a 5-slice window; psi_inv, rho and S with a 1-voxel halo and a
+// 3-slice window) are staged in shared-memory ring buffers by cp.async one slice
+// ahead of the compute, so the stencil reads are shared-memory loads and the global
+// traffic is one coalesced pass per field.  T o psi_inv and L o psi_inv are gathered
+// from the interleaved LT field (eight 16-byte loads per voxel).
 // ----------------------------------------------------------------------------------
+namespace {
+constexpr int kVH = 2, kVW = kTileX + 2 * kVH, kVR = kTileY + 2 * kVH, kVS = 7;  // v: halo, width, rows, slots
+constexpr int kQH = 1, kQW = kTileX + 2 * kQH, kQR = kTileY + 2 * kQH, kQS = 5;  // psi_inv, rho, S
+constexpr int kVPlane = kVW * kVR, kQPlane = kQW * kQR;
+constexpr int kPassASmemFloats = 3 * kVS * kVPlane + 5 * kQS * kQPlane;  // v x3, psi_inv x3, rho, S
+constexpr size_t kPassASmemBytes = sizeof(float) * kPassASmemFloats;
+
+struct PassASmem {
+    float* v;  // [3][kVS][kVR][kVW]
+    float* q;  // [3][kQS][kQR][kQW]
+    float* r;  // [kQS][kQR][kQW]
+    float* s;  // [kQS][kQR][kQW]
+};
+
+// stage one slice zs of a plane with halo h (rows kTileY + 2h, columns 32 + 2h) into
+// dst; cells outside the volume are not loaded (no interior voxel reads them)
+template <int H>
+__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int X, int Y, int Z, int x0,
+                                            int y0, int zs) {
+    constexpr int W = kTileX + 2 * H, R = kTileY + 2 * H;
+    if (zs < 0 || zs >= Z) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int xa = x0 - H + lane, xb = x0 - H + 32 + lane;
+    const bool ina = xa >= 0 && xa < X, inb = lane < 2 * H && xb < X;
+    for (int r = warp; r < R; r += kTileY) {
+        const int y = y0 - H + r;
+        if (y < 0 || y >= Y) continue;
+        const float* row = src + (long long)X * (y + (long long)Y * zs);
+        if (ina) cp_async4(dst + r * W + lane, row + xa);
+        if (inb) cp_async4(dst + r * W + 32 + lane, row + xb);
+    }
+}
+}  // namespace
+
+size_t ref_pass_a_smem_bytes() { return kPassASmemBytes; }
+
 __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
+    extern __shared__ float smem[];
+    PassASmem sm;
+    sm.v = smem;
+    sm.q = sm.v + 3 * kVS * kVPlane;
+    sm.r = sm.q + 3 * kQS * kQPlane;
+    sm.s = sm.r + kQS * kQPlane;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const Tile tl = a.tiles[t];
-        if (a.stop[tl.x]) continue;
+        if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
-        const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
-        if (x < 1 || x > P.X - 2 || y < 1 || y > P.Y - 2) continue;
         const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y, N = (int)P.N;
+        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + kTileZ, Z - 1);
+        if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
         const long long NT = a.NT;
-        const float* __restrict__ S = a.S + P.off;
-        const float* __restrict__ T = a.T + P.off;
-        const float* __restrict__ rho = a.rho + P.off;
-        const float* __restrict__ V[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
-        const float* __restrict__ Q[3] = {a.pinv + P.off, a.pinv + NT + P.off, a.pinv + 2 * NT + P.off};
-        const float* __restrict__ Lp[3] = {a.L + P.off, a.L + NT + P.off, a.L + 2 * NT + P.off};
+        const float* __restrict__ Vg[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
+        const float* __restrict__ Qg[3] = {a.pinv + P.off, a.pinv + NT + P.off, a.pinv + 2 * NT + P.off};
+        const float* __restrict__ Rg = a.rho + P.off;
+        const float* __restrict__ Sg = a.S + P.off;
+        const float* __restrict__ Tg = a.T + P.off;
+        const float4* __restrict__ LT = a.LT + P.off;
         float* rho_n = a.rho_n + P.off;
         float* Vn[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
         float* Qn[3] = {a.pinv_n + P.off, a.pinv_n + NT + P.off, a.pinv_n + 2 * NT + P.off};
+        const int x0 = tl.y, y0 = tl.z;
+        const int x = x0 + tx, y = y0 + ty;
+        const bool active = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
         const bool dv_xy = x >= 2 && x <= X - 3 && y >= 2 && y <= Y - 2;
-        const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, Z - 1);
-        for (int z = z0; z < z1; ++z) {
-            const int i = x + X * y + XY * z;
 
-            // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
-            const float q[3] = {__ldg(Q[0] + i), __ldg(Q[1] + i), __ldg(Q[2] + i)};
-            const Cell32 cl = locate32(X, Y, Z, q[0], q[1], q[2]);
-            const float Tq = a.first_iter ? __ldg(T + i) : tri_unchecked32(T, X, XY, N, cl);
-            float Lq[3];
+        auto vslot = [](int zs) { return ((zs % kVS) + kVS) % kVS; };
+        auto qslot = [](int zs) { return ((zs % kQS) + kQS) % kQS; };
+        auto stage_v = [&](int zs) {
+            const int sl = vslot(zs);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) Lq[c] = tri_unchecked32(Lp[c], X, XY, N, cl);
-
-            // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
-            float M[3][3];
+            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], X, Y, Z, x0, y0, zs);
+        };
+        auto stage_q = [&](int zs) {
+            const int sl = qslot(zs);
 #pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                M[r][0] = (__ldg(Q[r] + i + 1) - __ldg(Q[r] + i - 1)) * 0.5f;
-                M[r][1] = (__ldg(Q[r] + i + X) - __ldg(Q[r] + i - X)) * 0.5f;
-                M[r][2] = (__ldg(Q[r] + i + XY) - __ldg(Q[r] + i - XY)) * 0.5f;
-            }
-            const float det = det_ref(M);
+            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], X, Y, Z, x0, y0, zs);
+            stage_plane<kQH>(sm.r + sl * kQPlane, Rg, X, Y, Z, x0, y0, zs);
+            stage_plane<kQH>(sm.s + sl * kQPlane, Sg, X, Y, Z, x0, y0, zs);
+        };
 
-            // central-difference gradient of S and the potential gradient
-            const float Si = __ldg(S + i);
-            const float gs[3] = {(__ldg(S + i + 1) - __ldg(S + i - 1)) * 0.5f,
-                                 (__ldg(S + i + X) - __ldg(S + i - X)) * 0.5f,
-                                 (__ldg(S + i + XY) - __ldg(S + i - XY)) * 0.5f};
-            const float diff = Si - Tq;
-            float gU[3];
+        __syncthreads();  // the previous tile is done with the ring buffers
+        // prologue: everything slice zs0 needs, then what zs0 + 1 adds
+        for (int zs = zs0 - 2; zs <= zs0 + 2; ++zs) stage_v(zs);
+        for (int zs = zs0 - 1; zs <= zs0 + 1; ++zs) stage_q(zs);
+        cp_async_commit();
+        stage_v(zs0 + 3);
+        stage_q(zs0 + 2);
+        cp_async_commit();
+
+        // ring positions of slice z - 2 (v) and z - 1 (psi_inv, rho, S), advanced per slice
+        int sv = vslot(zs0 - 2), sq = qslot(zs0 - 1);
+        const int vc0 = (ty + kVH) * kVW + tx + kVH;
+        const int qc0 = (ty + kQH) * kQW + tx + kQH;
+        for (int z = zs0; z < zs1; ++z) {
+            cp_async_wait<1>();  // all but the newest group (slice z + 1's) have landed
+            __syncthreads();     // ... for every thread, and slice z - 3 / z - 2 is no longer read
+            // prefetch what slice z + 2 adds; with kVS = 7 and kQS = 5 slots the target
+            // slots are those of slices z - 3 (v) and z - 2 (the others)
+            if (z + 4 <= zs1 + 1) stage_v(z + 4);  // the last slice reads v up to zs1 + 1
+            if (z + 3 <= zs1) stage_q(z + 3);      // and psi_inv, rho, S up to zs1
+            cp_async_commit();
+            if (active) {
+                const int i = x + X * y + XY * z;
+                // per-slice base pointers into the rings (immediate offsets below)
+                const float* vb[5][3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (a.w_reg * Lq[c])) * det;
-
-            // velocity and its 6 neighbours, each loaded once
-            float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
+                for (int k = 0; k < 5; ++k) {
+                    int sl = sv + k;
+                    sl = sl >= kVS ? sl - kVS : sl;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                vc[c] = __ldg(V[c] + i);
-                vxm[c] = __ldg(V[c] + i - 1);
-                vxp[c] = __ldg(V[c] + i + 1);
-                vym[c] = __ldg(V[c] + i - X);
-                vyp[c] = __ldg(V[c] + i + X);
-                vzm[c] = __ldg(V[c] + i - XY);
-                vzp[c] = __ldg(V[c] + i + XY);
-            }
-            const float vx = vc[0], vy = vc[1], vz = vc[2];
+                    for (int c = 0; c < 3; ++c) vb[k][c] = sm.v + (c * kVS + sl) * kVPlane + vc0;
+                }
+                const float* qb[3][3];
+                const float* rb[3];
+                const float* sb[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    int sl = sq + k;
+                    sl = sl >= kQS ? sl - kQS : sl;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) qb[k][c] = sm.q + (c * kQS + sl) * kQPlane + qc0;
+                    rb[k] = sm.r + sl * kQPlane + qc0;
+                    sb[k] = sm.s + sl * kQPlane + qc0;
+                }
 
-            // divergence of rho*v (upwind) and the density update
-            const float p = __ldg(rho + i);
-            const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * __ldg(rho + i + 1);
-            const float t12 = (vxm[0] > 0.f) ? vxm[0] * __ldg(rho + i - 1) : vxm[0] * p;
-            const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * __ldg(rho + i + X);
-            const float t22 = (vym[1] > 0.f) ? vym[1] * __ldg(rho + i - X) : vym[1] * p;
-            const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * __ldg(rho + i + XY);
-            const float t32 = (vzm[2] > 0.f) ? vzm[2] * __ldg(rho + i - XY) : vzm[2] * p;
-            const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
-            const float rho_new = p + a.alpha * div;
-            rho_n[i] = rho_new;
+                // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
+                const float q[3] = {qb[1][0][0], qb[1][1][0], qb[1][2][0]};
+                const Cell32 cl = locate32(X, Y, Z, q[0], q[1], q[2]);
+                const float4 lt = tri_unchecked32_f4(LT, X, XY, N, cl);
+                const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
+                const float Lq[3] = {lt.x, lt.y, lt.z};
 
-            // (Dv)v: entropy scheme on the diagonal, upwind off the diagonal
-            const float ax1 = entropy_flux(vx, vxp[0]);
-            const float ax2 = (vy > 0.f) ? vy * (vx - vym[0]) : vy * (vyp[0] - vx);
-            const float ax3 = (vz > 0.f) ? vz * (vx - vzm[0]) : vz * (vzp[0] - vx);
-            const float ay1 = (vx > 0.f) ? vx * (vy - vxm[1]) : vx * (vxp[1] - vy);
-            const float ay2 = entropy_flux(vy, vyp[1]);
-            const float ay3 = (vz > 0.f) ? vz * (vy - vzm[1]) : vz * (vzp[1] - vy);
-            const float az1 = (vx > 0.f) ? vx * (vz - vxm[2]) : vx * (vxp[2] - vz);
-            const float az2 = (vy > 0.f) ? vy * (vz - vym[2]) : vy * (vyp[2] - vz);
-            const float az3 = entropy_flux(vz, vzp[2]);
-            const float dvv[3] = {(0.5f * ax1 + ax2) + ax3, (ay1 + 0.5f * ay2) + ay3, (az1 + az2) + 0.5f * az3};
+                // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
+                float M[3][3];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    M[r][0] = (qb[1][r][1] - qb[1][r][-1]) * 0.5f;
+                    M[r][1] = (qb[1][r][kQW] - qb[1][r][-kQW]) * 0.5f;
+                    M[r][2] = (qb[2][r][0] - qb[0][r][0]) * 0.5f;
+                }
+                const float det = det_ref(M);
 
-            // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
-            // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
-            // reference does, and y+2 at y = Y-2 reads linear index i + 2X as is.
-            float dv[3] = {0.f, 0.f, 0.f};
-            if (dv_xy && z >= 2 && z <= Z - 3) {
+                // central-difference gradient of S and the potential gradient
+                const float Si = sb[1][0];
+                const float gs[3] = {(sb[1][1] - sb[1][-1]) * 0.5f, (sb[1][kQW] - sb[1][-kQW]) * 0.5f,
+                                     (sb[2][0] - sb[0][0]) * 0.5f};
+                const float diff = Si - Tq;
+                float gU[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (a.w_reg * Lq[c])) * det;
+
+                // velocity and its 6 neighbours (vb[2] is slice z)
+                float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float xx = (vx < 0.f) ? (__ldg(V[c] + i + 2) - 2.f * vxp[c]) + vc[c]
-                                                : (vc[c] - 2.f * vxm[c]) + __ldg(V[c] + i - 2);
-                    const float yy = (vy < 0.f) ? (__ldg(V[c] + i + 2 * X) - 2.f * vym[c]) + vc[c]
-                                                : (vc[c] - 2.f * vym[c]) + __ldg(V[c] + i - 2 * X);
-                    const float zz = (vz < 0.f) ? (__ldg(V[c] + i + 2 * XY) - 2.f * vzm[c]) + vc[c]
-                                                : (vc[c] - 2.f * vzm[c]) + __ldg(V[c] + i - 2 * XY);
-                    dv[c] = -1.f * ((xx + yy) + zz);
+                    vc[c] = vb[2][c][0];
+                    vxm[c] = vb[2][c][-1];
+                    vxp[c] = vb[2][c][1];
+                    vym[c] = vb[2][c][-kVW];
+                    vyp[c] = vb[2][c][kVW];
+                    vzm[c] = vb[1][c][0];
+                    vzp[c] = vb[3][c][0];
+                }
+                const float vx = vc[0], vy = vc[1], vz = vc[2];
+
+                // divergence of rho*v (upwind) and the density update
+                const float p = rb[1][0];
+                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * rb[1][1];
+                const float t12 = (vxm[0] > 0.f) ? vxm[0] * rb[1][-1] : vxm[0] * p;
+                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * rb[1][kQW];
+                const float t22 = (vym[1] > 0.f) ? vym[1] * rb[1][-kQW] : vym[1] * p;
+                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * rb[2][0];
+                const float t32 = (vzm[2] > 0.f) ? vzm[2] * rb[0][0] : vzm[2] * p;
+                const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
+                const float rho_new = p + a.alpha * div;
+                rho_n[i] = rho_new;
+
+                // (Dv)v: entropy scheme on the diagonal, upwind off the diagonal
+                const float ax1 = entropy_flux(vx, vxp[0]);
+                const float ax2 = (vy > 0.f) ? vy * (vx - vym[0]) : vy * (vyp[0] - vx);
+                const float ax3 = (vz > 0.f) ? vz * (vx - vzm[0]) : vz * (vzp[0] - vx);
+                const float ay1 = (vx > 0.f) ? vx * (vy - vxm[1]) : vx * (vxp[1] - vy);
+                const float ay2 = entropy_flux(vy, vyp[1]);
+                const float ay3 = (vz > 0.f) ? vz * (vy - vzm[1]) : vz * (vzp[1] - vy);
+                const float az1 = (vx > 0.f) ? vx * (vz - vxm[2]) : vx * (vxp[2] - vz);
+                const float az2 = (vy > 0.f) ? vy * (vz - vym[2]) : vy * (vyp[2] - vz);
+                const float az3 = entropy_flux(vz, vzp[2]);
+                const float dvv[3] = {(0.5f * ax1 + ax2) + ax3, (ay1 + 0.5f * ay2) + ay3,
+                                      (az1 + az2) + 0.5f * az3};
+
+                // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
+                // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
+                // reference does; y+2 at y = Y-2 reads linear index i + 2X (voxel
+                // (x, 0, z+1)) from global memory, as the reference's unchecked read does
+                float dv[3] = {0.f, 0.f, 0.f};
+                if (dv_xy && z >= 2 && z <= Z - 3) {
+                    const bool y_edge = y + 2 > Y - 1;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float xx = (vx < 0.f) ? (vb[2][c][2] - 2.f * vxp[c]) + vc[c]
+                                                    : (vc[c] - 2.f * vxm[c]) + vb[2][c][-2];
+                        const float vyp2 = y_edge ? __ldg(Vg[c] + i + 2 * X) : vb[2][c][2 * kVW];
+                        const float yy = (vy < 0.f) ? (vyp2 - 2.f * vym[c]) + vc[c]
+                                                    : (vc[c] - 2.f * vym[c]) + vb[2][c][-2 * kVW];
+                        const float zz = (vz < 0.f) ? (vb[4][c][0] - 2.f * vzm[c]) + vc[c]
+                                                    : (vc[c] - 2.f * vzm[c]) + vb[0][c][0];
+                        dv[c] = -1.f * ((xx + yy) + zz);
+                    }
+                }
+
+                // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
+                const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);
+                float vn[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float friction = a.f1 * vc[c];
+                    const float diffusion = a.tau * dv[c];
+                    const float potential = qd * gU[c];
+                    const float acc = ((friction + dvv[c]) - diffusion) + potential;
+                    vn[c] = vc[c] - a.alpha * acc;
+                    Vn[c][i] = vn[c];
+                }
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float jv = ((M[r][0] * vn[0]) + (M[r][1] * vn[1])) + (M[r][2] * vn[2]);
+                    Qn[r][i] = q[r] - a.alpha * jv;
                 }
             }
-
-            // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
-            const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);
-            float vn[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float friction = a.f1 * vc[c];
-                const float diffusion = a.tau * dv[c];
-                const float potential = qd * gU[c];
-                const float acc = ((friction + dvv[c]) - diffusion) + potential;
-                vn[c] = vc[c] - a.alpha * acc;
-                Vn[c][i] = vn[c];
-            }
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                const float jv = ((M[r][0] * vn[0]) + (M[r][1] * vn[1])) + (M[r][2] * vn[2]);
-                Qn[r][i] = q[r] - a.alpha * jv;
-            }
+            sv = sv + 1 == kVS ? 0 : sv + 1;
+            sq = sq + 1 == kQS ? 0 : sq + 1;
         }
+        cp_async_wait<0>();
     }
 }
 
 // ----------------------------------------------------------------------------------
 // pass B: psi += alpha * v o psi, max update norm, convergence
 // ----------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) ref_pass_b_kernel(RefIterArgs a) {
+__global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
     __shared__ unsigned long long red[32];
     __shared__ bool last;
     const int tid = threadIdx.x;

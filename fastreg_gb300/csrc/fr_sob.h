@@ -19,7 +19,7 @@ namespace frg {
 
 constexpr int kMaxSmoothWidth = 15;
 constexpr int kSobTileY = 8;
-constexpr int kSobTileZ = 8;
+constexpr int kSobTileZ = 16;
 // the start/end kernels walk sobolev tiles with the reference tile extents
 static_assert(kSobTileY == kTileY && kSobTileZ == kTileZ, "tile extents must agree");
 

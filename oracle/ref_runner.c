@@ -91,10 +91,12 @@ typedef struct {
 
 /* Runs one registration with the reference kernels.  Host arrays: T/S float[N],
  * labels short[N]; outputs as for FastReg::operator(); psi/psi_inv 3 planes of N;
- * trace_norm/trace_idx hold one entry per iteration.  Returns iterations run, or -1. */
+ * trace_norm/trace_idx hold one entry per iteration; ms_out (may be NULL) receives the
+ * device-event time of FastReg::operator() from the input upload to the last apply
+ * ([0]) and of estimate_psi alone ([1]).  Returns iterations run, or -1. */
 int rr_register(const char *cubin_dir, const int *dims, const rr_params *P, const float *T, const short *labT,
                 const float *S, const short *labS, float *out_T, short *out_labT, float *out_S, short *out_labS,
-                float *psi_out, float *psi_inv_out, float *trace_norm, long long *trace_idx) {
+                float *psi_out, float *psi_inv_out, float *trace_norm, long long *trace_idx, float *ms_out) {
     CUmodule mods[M_COUNT] = {0};
     CUdeviceptr bufs[32];
     int nbufs = 0;
@@ -231,6 +233,10 @@ int rr_register(const char *cubin_dir, const int *dims, const rr_params *P, cons
     }
 
     /* ---- FastReg::operator(): pack the inputs ---- */
+    CUevent ev[3] = {0, 0, 0};
+    for (int k = 0; k < 3; ++k) CK(cuEventCreate(&ev[k], CU_EVENT_DEFAULT));
+    CK(cuStreamSynchronize(st));
+    CK(cuEventRecord(ev[0], st));
     CK(cuMemcpyHtoD(d_img_T, T, N * 4));
     CK(cuMemcpyHtoD(d_lab_T, labT, N * 2));
     CK(cuMemcpyHtoD(d_img_S, S, N * 4));
@@ -247,6 +253,7 @@ int rr_register(const char *cubin_dir, const int *dims, const rr_params *P, cons
     }
 
     /* ---- estimate_psi ---- */
+    CK(cuEventRecord(ev[1], st));
     {
         void *ag[] = {&vn, &fgrad}; /* VolumeDifferentiator{phi_n} */
         CK(launch2d(k_grad, X, Y, 64, 16, st, ag));
@@ -310,7 +317,13 @@ int rr_register(const char *cubin_dir, const int *dims, const rr_params *P, cons
         void *a_ap[] = {&vn, &vnw, &fpsi};
         CK(launch2d(k_apply, X, Y, 32, 16, st, a_ap));
     }
+    CK(cuEventRecord(ev[2], st));
     CK(cuStreamSynchronize(st));
+    if (ms_out) {
+        CK(cuEventElapsedTime(&ms_out[0], ev[0], ev[2]));
+        CK(cuEventElapsedTime(&ms_out[1], ev[1], ev[2]));
+    }
+    for (int k = 0; k < 3; ++k) cuEventDestroy(ev[k]);
 
     /* ---- get_image_data: float2 -> float + (short) label ---- */
     free(h_f2);

@@ -34,8 +34,10 @@ def _lib():
     return lib
 
 
-def register(params, T, labT, S, labS):
-    """One registration with the reference kernels; params has the Params fields."""
+def register(params, T, labT, S, labS, timing=False):
+    """One registration with the reference kernels; params has the Params fields.
+    With timing=True the result also holds ms_operator (device time of the whole
+    FastReg::operator() sequence, input upload to the last warp) and ms_estimate_psi."""
     lib = _lib()
     T = np.ascontiguousarray(T, np.float32)
     S = np.ascontiguousarray(S, np.float32)
@@ -52,10 +54,15 @@ def register(params, T, labT, S, labS):
     n = max(int(params.max_iter), 1)
     tn = np.zeros(n, np.float32)
     ti = np.zeros(n, np.int64)
+    ms = np.zeros(2, np.float32)
     p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
     ran = lib.rr_register(str(REF_DIR).encode(), dims, C.byref(P), p(T), p(labT), p(S), p(labS), p(oT), p(olT),
-                          p(oS), p(olS), p(psi), p(pinv), p(tn), p(ti))
+                          p(oS), p(olS), p(psi), p(pinv), p(tn), p(ti), p(ms))
     if ran < 0:
         raise RuntimeError("reference run failed: " + lib.rr_last_error().decode())
-    return dict(out_T=oT, out_labT=olT, out_S=oS, out_labS=olS, psi=psi, psi_inv=pinv, iterations=int(ran),
-                trace_norm=tn[:ran], trace_idx=ti[:ran])
+    out = dict(out_T=oT, out_labT=olT, out_S=oS, out_labS=olS, psi=psi, psi_inv=pinv, iterations=int(ran),
+               trace_norm=tn[:ran], trace_idx=ti[:ran])
+    if timing:
+        out["ms_operator"] = float(ms[0])
+        out["ms_estimate_psi"] = float(ms[1])
+    return out

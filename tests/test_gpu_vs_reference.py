@@ -1,0 +1,69 @@
+"""The full-size drop-in workload against the reference's own CUDA kernels.
+
+Runs the reference's kernels (compiled from its sources for sm_103a, launched in its
+order by oracle/ref_runner.c) and this library on the 182x218x182 synthetic pair with
+the reference's params.ini values for 200 iterations, on the same GB300:
+  - parity at full size: psi, psi_inv, both warped images and both warped label maps
+    bit for bit;
+  - speed: the whole FastReg::operator() of the reference (its 13 launches and two
+    host synchronisations per iteration) against fr_register, both timed with device
+    events; this library must be faster.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from fastreg_gb300 import FastReg, Params, _native as N, synthetic as sy
+from oracle import ref_runner
+from tests.helpers import assert_bitexact
+
+pytestmark = pytest.mark.gpu
+
+
+def test_full_size_parity_and_speed_against_reference_kernels(cuda):
+    import torch
+    if not ref_runner.available():
+        pytest.fail("reference kernels (oracle/_ref/*.cubin) are missing; build them with oracle/ref_build.py")
+    d = sy.make_pair(sy.CFG2)
+    dims = sy.CFG2.dims
+    P = Params(volume_dims=dims, no_labels=8, max_iter=200, alpha=0.004, tau=0.2, w_reg=0.2, rho_0=1.0, p=2.0,
+               C=0.25, reset_iter=-1, max_update_norm=-1e-10)
+    ref = ref_runner.register(P, d["T"], d["labT"], d["S"], d["labS"], timing=True)
+    ref2 = ref_runner.register(P, d["T"], d["labT"], d["S"], d["labS"], timing=True)
+
+    fr = FastReg(P)
+    pristine = [torch.from_numpy(d[k]).to(cuda) for k in ("T", "labT", "S", "labS")]
+    work = [t.clone() for t in pristine]
+    times = []
+    for rep in range(4):
+        for w, p in zip(work, pristine):
+            w.copy_(p)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fr(*work, sync=False)
+        e1.record()
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ours_ms = float(np.median(times[1:]))
+    ref_ms = min(ref["ms_operator"], ref2["ms_operator"])
+
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), ref["psi"], "psi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy(), ref["psi_inv"], "psi_inv")
+    assert_bitexact(work[0].cpu().numpy(), ref["out_T"], "T o psi_inv")
+    assert_bitexact(work[2].cpu().numpy(), ref["out_S"], "S o psi")
+    assert_bitexact(work[1].cpu().numpy(), ref["out_labT"], "labels T o psi_inv")
+    assert_bitexact(work[3].cpu().numpy(), ref["out_labS"], "labels S o psi")
+
+    record = {"workload": "182x218x182, 200 iterations, reference params.ini values",
+              "reference_cuda_ms": ref_ms, "reference_cuda_estimate_psi_ms": ref["ms_estimate_psi"],
+              "fastreg_gb300_ms": ours_ms, "speedup": ref_ms / ours_ms}
+    print(json.dumps(record))
+    out = os.environ.get("FASTREG_RECORD_DIR")
+    if out:
+        with open(os.path.join(out, "vs_reference_cuda.json"), "w") as f:
+            json.dump(record, f)
+    assert ours_ms < ref_ms
+    fr.close()
