@@ -33,8 +33,8 @@ DIMS = (182, 218, 182)
 ITERS = 200
 
 # algorithmic bytes per interior voxel and launch (packed FP32: vector 12 B, scalar 4 B)
-BYTES_LAPLACIAN = 12 + 12           # psi read, L written
-BYTES_PASS_A = 4 + 12 + 12 + 12 + 4 + 4 + 4 + 12 + 12  # rho, v, psi_inv, L o psi_inv, S, T o psi_inv; rho, v, psi_inv
+BYTES_LAPLACIAN = 12 + 4 + 16       # psi and T read, (L, T) interleaved written
+BYTES_PASS_A = 4 + 12 + 12 + 16 + 4 + 4 + 12 + 12  # rho, v, psi_inv, (L, T) o psi_inv, S; rho, v, psi_inv
 BYTES_PASS_B = 12 + 12 + 12         # psi, v o psi gathered, psi written
 BYTES_ITER_CANONICAL = 112          # per voxel-iteration with L recomputed from psi (no L round trip)
 BYTES_WARP = 12 + 4 + 4 + 2 + 2     # psi, image gathered, out, label gathered, out label

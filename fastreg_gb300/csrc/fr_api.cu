@@ -280,7 +280,7 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, ntiles);
     } else {
         h->grid_a = occupancy_grid(h, (const void*)frg::sob_grad_kernel, ntiles);
-        h->grid_lap = occupancy_grid(h, (const void*)frg::sob_smooth_kernel, ntiles);
+        h->grid_lap = occupancy_grid(h, frg::sob_smooth3_fn(h->P.smooth_width / 2), ntiles);
         h->grid_b = occupancy_grid(h, (const void*)frg::sob_pass_b_kernel, ntiles);
     }
     h->grid_io = occupancy_grid(h, (const void*)frg::finalize_kernel, ntiles);
@@ -337,7 +337,7 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
 }
 
 // kernels launched per iteration
-int kernels_per_iter(const fr_handle* h) { return h->P.solver == FR_SOLVER_REFERENCE ? 3 : 5; }
+int kernels_per_iter(const fr_handle* h) { return 3; }
 
 int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev = nullptr) {
     if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
@@ -352,7 +352,6 @@ int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev
     a.phi = h->psi;
     a.m = h->v[0];
     a.g = h->grad;
-    a.tmp = h->v[1];
     a.damping = h->P.damping;
     a.step = h->P.step;
     frg::gaussian_taps(h->P.smooth_sigma, h->P.smooth_width, a.taps);

@@ -1,8 +1,8 @@
 // fr_sob.cu -- kernels of the sobolev solver (see fr_sob.h for the iteration).
 //
 // Launches per iteration: sob_grad_kernel (W, residual, exact trilinear gradient,
-// FP64 data energy), three sob_smooth_kernel passes (x, y, then z fused with the
-// momentum update), sob_pass_b_kernel (compositional update, max update norm,
+// FP64 data energy), sob_smooth3_kernel (separable Gaussian along x, y, z fused with
+// the momentum update), sob_pass_b_kernel (compositional update, max update norm,
 // on-device convergence test).
 #include <cmath>
 
@@ -58,16 +58,21 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         double e = 0.0;
         if (x < P.X && y < P.Y) {
-            const long long NT = a.NT, X = P.X, XY = (long long)P.X * P.Y;
+            const long long NT = a.NT;
+            const int X = P.X, XY = P.X * P.Y;
             const float* __restrict__ S = a.S + P.off;
             const float* __restrict__ T = a.T + P.off;
-            const float* __restrict__ phi = a.phi + P.off;
-            float* g = a.g + P.off;
+            const float* __restrict__ phi0 = a.phi + P.off;
+            const float* __restrict__ phi1 = phi0 + NT;
+            const float* __restrict__ phi2 = phi1 + NT;
+            float* g0 = a.g + P.off;
+            float* g1 = g0 + NT;
+            float* g2 = g1 + NT;
             const int z1 = min(tl.w + kSobTileZ, P.Z);
             for (int z = tl.w; z < z1; ++z) {
-                const long long i = lin(P, x, y, z);
-                const SobCell s = sob_locate(P, __ldg(phi + i), __ldg(phi + NT + i), __ldg(phi + 2 * NT + i));
-                const long long b = s.base;
+                const int i = x + X * y + XY * z;
+                const SobCell s = sob_locate(P, __ldg(phi0 + i), __ldg(phi1 + i), __ldg(phi2 + i));
+                const int b = (int)s.base;
                 const float f000 = __ldg(S + b), f100 = __ldg(S + b + 1);
                 const float f010 = __ldg(S + b + X), f110 = __ldg(S + b + 1 + X);
                 const float f001 = __ldg(S + b + XY), f101 = __ldg(S + b + 1 + XY);
@@ -82,9 +87,9 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                                                   lerpf_(f011 - f010, f001 - f000, s.b), s.a)
                                          : 0.f;
                 const float r = W - __ldg(T + i);
-                g[i] = r * dWa;
-                g[NT + i] = r * dWb;
-                g[2 * NT + i] = r * dWc;
+                g0[i] = r * dWa;
+                g1[i] = r * dWb;
+                g2[i] = r * dWc;
                 e += (double)r * (double)r;
             }
         }
@@ -93,41 +98,88 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
     }
 }
 
-// One separable pass along `axis` (0 = x, 1 = y, 2 = z) with the replicate boundary;
-// with `momentum` set the result gs updates m = damping * m - step * gs instead of
-// being stored.
-__global__ void __launch_bounds__(256) sob_smooth_kernel(SobIterArgs a, int axis, const float* src, float* dst,
-                                                         int momentum) {
+// Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
+// fused with the momentum update m = damping * m - step * gs.  A block owns a 32 x 8
+// column tile: each input slice (tile + R halo, coordinates clamped into the volume)
+// is staged in shared memory by cp.async one slice ahead, smoothed along x and y in
+// shared memory, and pushed into a per-thread register ring of 2R + 1 slices that the
+// z pass reads.  Each tap is one fused multiply-add, acc = fma(w_k, g_k, acc), taken
+// in the order k = -R..R for every axis.
+template <int R>
+__global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
+    constexpr int W = kTileX + 2 * R, H = kSobTileY + 2 * R, K = 2 * R + 1;
+    __shared__ float G[2][3][H][W];
+    __shared__ float Gx[3][H][kTileX];
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    float taps[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) taps[k] = a.taps[k];
+
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const Tile tl = a.tiles[t];
-        if (a.stop[tl.x]) continue;
+        if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
-        const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
-        if (x >= P.X || y >= P.Y) continue;
+        const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y;
         const long long NT = a.NT;
-        const int R = a.radius;
-        const int z1 = min(tl.w + kSobTileZ, P.Z);
-        const int dim = axis == 0 ? P.X : (axis == 1 ? P.Y : P.Z);
-        const long long stride = axis == 0 ? 1 : (axis == 1 ? (long long)P.X : (long long)P.X * P.Y);
-        for (int z = tl.w; z < z1; ++z) {
-            const long long i = lin(P, x, y, z);
-            const int pos = axis == 0 ? x : (axis == 1 ? y : z);
+        const float* __restrict__ g[3] = {a.g + P.off, a.g + NT + P.off, a.g + 2 * NT + P.off};
+        float* m[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
+        const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + kSobTileZ, Z);
+        const int nsl = (zt1 - zt0) + 2 * R;
+
+        auto stage = [&](int zs, int buf) {
+            const int zc = min(max(zs, 0), Z - 1);
+            for (int e = tid; e < 3 * H * W; e += 256) {
+                const int c = e / (H * W), rem = e - c * (H * W), r = rem / W, col = rem - r * W;
+                const int gx = min(max(x0 - R + col, 0), X - 1), gy = min(max(y0 - R + r, 0), Y - 1);
+                cp_async4(&G[buf][c][r][col], g[c] + gx + X * gy + XY * zc);
+            }
+        };
+
+        float ring[K][3];
+        __syncthreads();  // the previous tile is done with G and Gx
+        stage(zt0 - R, 0);
+        cp_async_commit();
+        for (int k = 0; k < nsl; ++k) {
+            const int zs = zt0 - R + k, buf = k & 1;
+            if (k + 1 < nsl) stage(zs + 1, buf ^ 1);
+            cp_async_commit();
+            cp_async_wait<1>();
+            __syncthreads();
+            // x pass over the tile rows and the y halo
+            for (int e = tid; e < 3 * H * kTileX; e += 256) {
+                const int c = e / (H * kTileX), rem = e - c * (H * kTileX), r = rem / kTileX, col = rem - r * kTileX;
+                float acc = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], G[buf][c][r][col + q], acc);
+                Gx[c][r][col] = acc;
+            }
+            __syncthreads();
+            // y pass for this thread's column, pushed into the z ring
+#pragma unroll
+            for (int q = 0; q < K - 1; ++q)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ring[q][c] = ring[q + 1][c];
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                const float* __restrict__ Sp = src + c * NT + P.off;
                 float acc = 0.f;
-                for (int k = -R; k <= R; ++k) {
-                    const int q = min(max(pos + k, 0), dim - 1);
-                    acc = acc + a.taps[k + R] * __ldg(Sp + i + (long long)(q - pos) * stride);
-                }
-                if (momentum) {
-                    float* mp = dst + c * NT + P.off;
-                    mp[i] = a.damping * mp[i] - a.step * acc;
-                } else {
-                    dst[c * NT + P.off + i] = acc;
+#pragma unroll
+                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], Gx[c][ty + q][tx], acc);
+                ring[K - 1][c] = acc;
+            }
+            // z pass and momentum for slice zs - R once the ring holds its 2R + 1 slices
+            const int x = x0 + tx, y = y0 + ty, zo = zs - R;
+            if (k >= 2 * R && x < X && y < Y) {
+                const int i = x + X * y + XY * zo;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int q = 0; q < K; ++q) acc = fmaf(taps[q], ring[q][c], acc);
+                    m[c][i] = a.damping * m[c][i] - a.step * acc;
                 }
             }
         }
+        cp_async_wait<0>();
     }
 }
 
@@ -141,28 +193,29 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         unsigned long long best = 0ull;
         if (x < P.X && y < P.Y) {
-            const long long NT = a.NT, X = P.X, XY = (long long)P.X * P.Y;
-            float* phi = a.phi + P.off;
-            const float* __restrict__ m = a.m + P.off;
+            const long long NT = a.NT;
+            const int X = P.X, XY = P.X * P.Y;
+            float* phi[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
+            const float* __restrict__ mc[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
             const int z1 = min(tl.w + kSobTileZ, P.Z);
             for (int z = tl.w; z < z1; ++z) {
-                const long long i = lin(P, x, y, z);
-                const float px = phi[i], py = phi[NT + i], pz = phi[2 * NT + i];
+                const int i = x + X * y + XY * z;
+                const float px = phi[0][i], py = phi[1][i], pz = phi[2][i];
                 const SobCell s = sob_locate(P, px, py, pz);
                 float u[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float* __restrict__ F = m + c * NT;
-                    const long long b = s.base;
+                    const float* __restrict__ F = mc[c];
+                    const int b = (int)s.base;
                     u[c] = lerpf_(lerpf_(lerpf_(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), s.c),
                                          lerpf_(__ldg(F + b + 1 + XY), __ldg(F + b + 1), s.c), s.b),
                                   lerpf_(lerpf_(__ldg(F + b + X + XY), __ldg(F + b + X), s.c),
                                          lerpf_(__ldg(F + b + XY), __ldg(F + b), s.c), s.b),
                                   s.a);
                 }
-                phi[i] = px + u[0];
-                phi[NT + i] = py + u[1];
-                phi[2 * NT + i] = pz + u[2];
+                phi[0][i] = px + u[0];
+                phi[1][i] = py + u[1];
+                phi[2][i] = pz + u[2];
                 const float nrm = norm3_rd(u[0], u[1], u[2]);
                 if (nrm == nrm) {
                     const unsigned long long k = norm_key(nrm, i);
@@ -193,15 +246,33 @@ cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t
     if (ev) cudaEventRecord(ev[0], s);
     sob_grad_kernel<<<grids[0], 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    sob_smooth_kernel<<<grids[1], 256, 0, s>>>(a, 0, a.g, a.tmp, 0);
+    switch (a.radius) {
+        case 0: sob_smooth3_kernel<0><<<grids[1], 256, 0, s>>>(a); break;
+        case 1: sob_smooth3_kernel<1><<<grids[1], 256, 0, s>>>(a); break;
+        case 2: sob_smooth3_kernel<2><<<grids[1], 256, 0, s>>>(a); break;
+        case 3: sob_smooth3_kernel<3><<<grids[1], 256, 0, s>>>(a); break;
+        case 4: sob_smooth3_kernel<4><<<grids[1], 256, 0, s>>>(a); break;
+        case 5: sob_smooth3_kernel<5><<<grids[1], 256, 0, s>>>(a); break;
+        case 6: sob_smooth3_kernel<6><<<grids[1], 256, 0, s>>>(a); break;
+        default: sob_smooth3_kernel<7><<<grids[1], 256, 0, s>>>(a); break;
+    }
     if (ev) cudaEventRecord(ev[2], s);
-    sob_smooth_kernel<<<grids[1], 256, 0, s>>>(a, 1, a.tmp, a.g, 0);
-    if (ev) cudaEventRecord(ev[3], s);
-    sob_smooth_kernel<<<grids[1], 256, 0, s>>>(a, 2, a.g, a.m, 1);
-    if (ev) cudaEventRecord(ev[4], s);
     sob_pass_b_kernel<<<grids[2], 256, 0, s>>>(a);
-    if (ev) cudaEventRecord(ev[5], s);
+    if (ev) cudaEventRecord(ev[3], s);
     return cudaGetLastError();
+}
+
+const void* sob_smooth3_fn(int radius) {
+    switch (radius) {
+        case 0: return (const void*)sob_smooth3_kernel<0>;
+        case 1: return (const void*)sob_smooth3_kernel<1>;
+        case 2: return (const void*)sob_smooth3_kernel<2>;
+        case 3: return (const void*)sob_smooth3_kernel<3>;
+        case 4: return (const void*)sob_smooth3_kernel<4>;
+        case 5: return (const void*)sob_smooth3_kernel<5>;
+        case 6: return (const void*)sob_smooth3_kernel<6>;
+        default: return (const void*)sob_smooth3_kernel<7>;
+    }
 }
 
 }  // namespace frg

@@ -6,7 +6,8 @@
 //   g(x)   = (W(x) - T(x)) * dW/dphi(x)        exact derivative of the trilinear
 //                                              interpolant (0 along a clamped axis)
 //   gs     = G_sigma * g                       separable Gaussian, SMOOTH_WIDTH taps,
-//                                              normalised, replicate boundary
+//                                              normalised, replicate boundary, each tap
+//                                              a fused multiply-add in the order -R..R
 //   m      = DAMPING * m - STEP * gs
 //   phi(x) = phi(x) + m(phi(x))                trilinear gather of the new m
 #pragma once
@@ -34,7 +35,6 @@ struct SobIterArgs {
     float* phi;   // positions (3 planes)
     float* m;     // momentum (3 planes)
     float* g;     // gradient (3 planes)
-    float* tmp;   // smoothing temporary (3 planes)
     float damping, step;
     float taps[kMaxSmoothWidth];
     int radius;
@@ -52,10 +52,10 @@ struct SobIterArgs {
 void gaussian_taps(float sigma, int width, float* taps);
 
 __global__ void sob_grad_kernel(SobIterArgs a);
-__global__ void sob_smooth_kernel(SobIterArgs a, int axis, const float* src, float* dst, int momentum);
+const void* sob_smooth3_fn(int radius);  // the smoothing kernel instance for a radius
 __global__ void sob_pass_b_kernel(SobIterArgs a);
 
-// grids: {grad, smooth, pass_b}; with `ev` (6 events) each launch is bracketed
+// grids: {grad, smooth, pass_b}; with `ev` (4 events) each launch is bracketed
 cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t s, cudaEvent_t* ev = nullptr);
 
 }  // namespace frg

@@ -136,7 +136,7 @@ int fr_finish(fr_handle *h, void *stream);                                  /* o
 /* ---- measurement: run `iters` iterations from the current state with CUDA events
  *      around every launch on `stream`; ms[k] = mean duration of kernel k of one
  *      iteration (reference solver: k = 0 Laplacian, 1 pass A, 2 pass B; sobolev:
- *      0 gradient, 1 smoothing x, 2 smoothing y, 3 smoothing z + momentum, 4 pass B);
+ *      0 gradient, 1 smoothing + momentum, 2 pass B);
  *      n_kernels receives the count.  No counterpart in the reference. ---- */
 int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *stream);
 

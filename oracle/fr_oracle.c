@@ -674,8 +674,8 @@ double FN(sob_grad)(const int *dims, const real *S, const real *T, const real *p
     return 0.5 * e;
 }
 
-/* one separable pass along axis with the replicate boundary; momentum != 0:
- * m = damping * m - step * (smoothed src) */
+/* one separable pass along axis with the replicate boundary, each tap a fused
+ * multiply-add in the order -R..R; momentum != 0: m = damping * m - step * (smoothed src) */
 void FN(sob_smooth)(const int *dims, const real *taps, int R_, int axis, const real *src, real *dst, int momentum,
                     real damping, real step) {
     fro_dims d = {dims[0], dims[1], dims[2]};
@@ -695,7 +695,7 @@ void FN(sob_smooth)(const int *dims, const real *taps, int R_, int axis, const r
                         int q = pos + k;
                         if (q < 0) q = 0;
                         if (q > dim - 1) q = dim - 1;
-                        acc = acc + taps[k + R_] * Sp[i + (int64_t)(q - pos) * stride];
+                        acc = FMA_(taps[k + R_], Sp[i + (int64_t)(q - pos) * stride], acc);
                     }
                     if (momentum)
                         dst[c * N + i] = damping * dst[c * N + i] - step * acc;
