@@ -219,6 +219,66 @@ def profile_case(args):
     return 0
 
 
+def batched_vs_plain(dev, stream, n_pairs=16, reps=2):
+    """One fr_register_batch over the uneven cohort against one fr_register per pair
+    (a handle per pair size), same data, same iterations; checks the two agree bit
+    for bit."""
+    import torch
+    from fastreg_gb300 import FastReg, synthetic as sy, _native as N
+    specs = sy.cohort_specs(n_pairs)
+    pristine = []
+    for sp in specs:
+        d = sy.make_pair_torch(sp, dev)
+        pristine.append((d["T"], d["labT"], d["S"], d["labS"]))
+    work = [tuple(t.clone() for t in q) for q in pristine]
+
+    def restore():
+        for w, p in zip(work, pristine):
+            for a, b in zip(w, p):
+                a.copy_(b, non_blocking=True)
+
+    P = reference_params(dims=specs[0].dims)
+    frb = FastReg(P)
+    plain = [FastReg(reference_params(dims=sp.dims)) for sp in specs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    tb, tp = [], []
+    with torch.cuda.stream(stream):
+        for rep in range(reps + 1):
+            restore()
+            e0.record(stream)
+            frb.register_batch(work, stream=stream, sync=False)
+            e1.record(stream)
+            stream.synchronize()
+            if rep:
+                tb.append(e0.elapsed_time(e1))
+        psi_b = [frb.get_field(N.FR_FIELD_PSI, pair=k) for k in range(n_pairs)]
+        lab_b = [w[3].clone() for w in work]
+        for rep in range(reps + 1):
+            restore()
+            e0.record(stream)
+            for fr, w in zip(plain, work):
+                fr(*w, stream=stream, sync=False)
+            e1.record(stream)
+            stream.synchronize()
+            if rep:
+                tp.append(e0.elapsed_time(e1))
+    same = all(torch.equal(psi_b[k], plain[k].get_field(N.FR_FIELD_PSI)) and torch.equal(lab_b[k], work[k][3])
+               for k in range(n_pairs))
+    ssd_b = [frb.stats(k).e_data for k in range(n_pairs)]
+    ssd_p = [plain[k].stats().e_data for k in range(n_pairs)]
+    voxels = sum(sp.dims[0] * sp.dims[1] * sp.dims[2] for sp in specs)
+    t_b, t_p = min(tb), min(tp)
+    for fr in plain:
+        fr.close()
+    frb.close()
+    return {"cohort": f"{n_pairs} pairs, dims per pair from {{96,128,160,192}}x{{112,160,224}}x{{96,128,192}}, "
+                      f"{voxels} voxels in total, reference solver, {ITERS} iterations",
+            "batched_pairs_per_s": n_pairs / (t_b / 1000.0), "plain_pairs_per_s": n_pairs / (t_p / 1000.0),
+            "ratio": t_p / t_b, "batched_ms": t_b, "plain_ms": t_p,
+            "bitexact_batched_vs_plain": bool(same),
+            "max_ssd_rel_diff": max(abs(a - b) / max(abs(b), 1e-30) for a, b in zip(ssd_b, ssd_p))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,6 +462,9 @@ def main():
                                                            data["S"].astype(np.float64)) ** 2).sum()),
                            "folds": ss.folds, "dice_all": ss.dice_all}
         frs.close()
+
+        # batched cohort against plain per-pair calls: 16 uneven pairs, 200 iterations each
+        line["batched"] = batched_vs_plain(dev, stream)
 
         # CPU baseline: the oracle port on the host cores, bounded sample
         cores = os.cpu_count() or 1

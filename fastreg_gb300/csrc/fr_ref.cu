@@ -337,9 +337,21 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
             const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
             float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
             const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
-            for (int z = z0; z < z1; ++z) {
-                const int i = x + X * y + XY * z;
-                const float px = Q[0][i], py = Q[1][i], pz = Q[2][i];
+            int i = x + X * y + XY * z0;
+            // psi of the next slice is loaded while this slice's gathers are in flight
+            float nx = 0.f, ny = 0.f, nz = 0.f;
+            if (z0 < z1) {
+                nx = Q[0][i];
+                ny = Q[1][i];
+                nz = Q[2][i];
+            }
+            for (int z = z0; z < z1; ++z, i += XY) {
+                const float px = nx, py = ny, pz = nz;
+                if (z + 1 < z1) {
+                    nx = Q[0][i + XY];
+                    ny = Q[1][i + XY];
+                    nz = Q[2][i + XY];
+                }
                 const Cell32 cl = locate32(X, Y, Z, px, py, pz);
                 const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, XY, cl);
                 const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, XY, cl);

@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
     constexpr int W = kTileX + 2 * R, H = kSobTileY + 2 * R, K = 2 * R + 1;
     __shared__ float G[2][3][H][W];
     __shared__ float Gx[3][H][kTileX];
-    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     float taps[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) taps[k] = a.taps[k];
@@ -126,12 +126,17 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
         const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + kSobTileZ, Z);
         const int nsl = (zt1 - zt0) + 2 * R;
 
+        // clamped x of this lane's staged columns (replicate boundary)
+        const int xa = min(max(x0 - R + tx, 0), X - 1);
+        const int xb = min(max(x0 - R + 32 + tx, 0), X - 1);
         auto stage = [&](int zs, int buf) {
             const int zc = min(max(zs, 0), Z - 1);
-            for (int e = tid; e < 3 * H * W; e += 256) {
-                const int c = e / (H * W), rem = e - c * (H * W), r = rem / W, col = rem - r * W;
-                const int gx = min(max(x0 - R + col, 0), X - 1), gy = min(max(y0 - R + r, 0), Y - 1);
-                cp_async4(&G[buf][c][r][col], g[c] + gx + X * gy + XY * zc);
+            for (int rr = ty; rr < 3 * H; rr += kSobTileY) {  // one row per warp
+                const int c = rr / H, r = rr - c * H;
+                const int gy = min(max(y0 - R + r, 0), Y - 1);
+                const float* row = g[c] + X * gy + XY * zc;
+                cp_async4(&G[buf][c][r][tx], row + xa);
+                if (tx < 2 * R) cp_async4(&G[buf][c][r][32 + tx], row + xb);
             }
         };
 
@@ -145,13 +150,13 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
             cp_async_commit();
             cp_async_wait<1>();
             __syncthreads();
-            // x pass over the tile rows and the y halo
-            for (int e = tid; e < 3 * H * kTileX; e += 256) {
-                const int c = e / (H * kTileX), rem = e - c * (H * kTileX), r = rem / kTileX, col = rem - r * kTileX;
+            // x pass over the tile rows and the y halo, one row per warp
+            for (int rr = ty; rr < 3 * H; rr += kSobTileY) {
+                const int c = rr / H, r = rr - c * H;
                 float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], G[buf][c][r][col + q], acc);
-                Gx[c][r][col] = acc;
+                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], G[buf][c][r][tx + q], acc);
+                Gx[c][r][tx] = acc;
             }
             __syncthreads();
             // y pass for this thread's column, pushed into the z ring
@@ -198,9 +203,16 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
             float* phi[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
             const float* __restrict__ mc[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
             const int z1 = min(tl.w + kSobTileZ, P.Z);
-            for (int z = tl.w; z < z1; ++z) {
-                const int i = x + X * y + XY * z;
-                const float px = phi[0][i], py = phi[1][i], pz = phi[2][i];
+            int i = x + X * y + XY * tl.w;
+            // phi of the next slice is loaded while this slice's gathers are in flight
+            float nx = phi[0][i], ny = phi[1][i], nz = phi[2][i];
+            for (int z = tl.w; z < z1; ++z, i += XY) {
+                const float px = nx, py = ny, pz = nz;
+                if (z + 1 < z1) {
+                    nx = phi[0][i + XY];
+                    ny = phi[1][i + XY];
+                    nz = phi[2][i + XY];
+                }
                 const SobCell s = sob_locate(P, px, py, pz);
                 float u[3];
 #pragma unroll

@@ -100,3 +100,73 @@ def cohort_dims(n_pairs: int, seed: int = 3000):
     rng = np.random.Generator(np.random.PCG64(seed))
     xs, ys, zs = (96, 128, 160, 192), (112, 160, 224), (96, 128, 192)
     return [(int(rng.choice(xs)), int(rng.choice(ys)), int(rng.choice(zs))) for _ in range(n_pairs)]
+
+
+def make_pair_torch(spec: PairSpec, device="cuda"):
+    """The same construction on the GPU with torch (for large cohorts in the benchmark;
+    the values differ from make_pair's in rounding).  Returns CUDA tensors T, labT, S,
+    labS of shape (Z, Y, X)."""
+    import torch
+    import torch.nn.functional as F
+
+    g = torch.Generator(device="cpu").manual_seed(int(spec.seed))
+    X, Y, Z = spec.dims
+    dev = torch.device(device)
+    zz = torch.arange(Z, device=dev, dtype=torch.float32)[:, None, None]
+    yy = torch.arange(Y, device=dev, dtype=torch.float32)[None, :, None]
+    xx = torch.arange(X, device=dev, dtype=torch.float32)[None, None, :]
+    T = torch.zeros((Z, Y, X), device=dev, dtype=torch.float32)
+    lo = torch.tensor([0.0, 0.0, 0.0])
+    hi = torch.tensor([X - 1.0, Y - 1.0, Z - 1.0])
+    for _ in range(spec.n_blobs):
+        c = lo + (hi - lo) * torch.rand(3, generator=g)
+        s = spec.sigma_range[0] + (spec.sigma_range[1] - spec.sigma_range[0]) * float(torch.rand(1, generator=g))
+        a = spec.amp_range[0] + (spec.amp_range[1] - spec.amp_range[0]) * float(torch.rand(1, generator=g))
+        inv = 1.0 / (2 * s * s)
+        T += a * (torch.exp(-(xx - float(c[0])) ** 2 * inv) * torch.exp(-(yy - float(c[1])) ** 2 * inv) *
+                  torch.exp(-(zz - float(c[2])) ** 2 * inv))
+    T = T.clamp(0.0, 1.0)
+    if spec.noise > 0:
+        T = T + spec.noise * torch.randn((Z, Y, X), generator=g).to(dev)
+
+    def smooth(vol, sigma):
+        r = int(3 * sigma + 0.5)
+        k = torch.exp(-torch.arange(-r, r + 1, dtype=torch.float32) ** 2 / (2 * sigma * sigma))
+        k = (k / k.sum()).to(dev)
+        v = vol[None, None]
+        v = F.conv3d(F.pad(v, (r, r, 0, 0, 0, 0), mode="replicate"), k.view(1, 1, 1, 1, -1))
+        v = F.conv3d(F.pad(v, (0, 0, r, r, 0, 0), mode="replicate"), k.view(1, 1, 1, -1, 1))
+        v = F.conv3d(F.pad(v, (0, 0, 0, 0, r, r), mode="replicate"), k.view(1, 1, -1, 1, 1))
+        return v[0, 0]
+
+    v = torch.stack([smooth(torch.randn((Z, Y, X), generator=g).to(dev), spec.vel_sigma) for _ in range(3)])
+    v *= spec.max_disp / v.pow(2).sum(0).sqrt().max().clamp_min(1e-12)
+
+    def sample(field, disp, mode):
+        # field (C, Z, Y, X); disp (3, Z, Y, X) in voxels, components (x, y, z)
+        px = (xx + disp[0]) * (2.0 / max(X - 1, 1)) - 1.0
+        py = (yy + disp[1]) * (2.0 / max(Y - 1, 1)) - 1.0
+        pz = (zz + disp[2]) * (2.0 / max(Z - 1, 1)) - 1.0
+        grid = torch.stack([px, py, pz], dim=-1)[None]
+        return F.grid_sample(field[None], grid, mode=mode, padding_mode="border", align_corners=True)[0]
+
+    u = v / (2 ** spec.squarings)
+    for _ in range(spec.squarings):
+        u = u + sample(u, u, "bilinear")
+    S = sample(T[None], u, "bilinear")[0]
+    thr = torch.arange(1, spec.n_classes, device=dev, dtype=torch.float32) / spec.n_classes
+    labT = torch.bucketize(T.clamp(0.0, 1.0), thr, right=True).to(torch.int16)
+    labS = sample(labT[None].float(), u, "nearest")[0].to(torch.int16)
+    return dict(T=T.contiguous(), labT=labT.contiguous(), S=S.contiguous(), labS=labS.contiguous())
+
+
+def cohort_specs(n_pairs: int = 16, seed: int = 3000):
+    """The uneven batched cohort: dims drawn per pair (cohort_dims), blobs scaled with
+    the volume, maximum displacement uniform in [2, 6] voxels, one seed per pair."""
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    specs = []
+    for k, d in enumerate(cohort_dims(n_pairs, seed)):
+        n = d[0] * d[1] * d[2]
+        specs.append(PairSpec(dims=d, n_blobs=max(40, n // 20000), vel_sigma=4.0,
+                              max_disp=float(rng.uniform(2.0, 6.0)), n_classes=4, seed=seed + 100 + k))
+    return specs
