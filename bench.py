@@ -219,6 +219,33 @@ def profile_case(args):
     return 0
 
 
+def adjoint_timing(dev, stream, reps=3):
+    import ctypes as C
+    import torch
+    from fastreg_gb300 import synthetic as sy, _native as N
+    lib = N.load()
+    spec = sy.PairSpec(dims=(128, 128, 128), n_blobs=40, vel_sigma=4.0, max_disp=4.0, n_classes=4, seed=4000)
+    d = sy.make_pair_torch(spec, dev)
+    g = torch.Generator(device="cpu").manual_seed(4001)
+    v0 = (0.05 * torch.randn((3, 128, 128, 128), generator=g)).to(dev)
+    gv = torch.empty_like(v0)
+    dims = (C.c_int * 3)(128, 128, 128)
+    loss, gl = C.c_double(), C.c_double()
+    P = reference_params(dims=(128, 128, 128), solver="sobolev")
+    times = []
+    for rep in range(reps + 1):
+        t0 = time.perf_counter()
+        rc = lib.fr_sobolev_loss_grad(d["T"].data_ptr(), d["S"].data_ptr(), dims, v0.data_ptr(), 0.2, 50, 10,
+                                      P.damping, P.step, P.smooth_sigma, P.smooth_width, C.byref(loss),
+                                      gv.data_ptr(), C.byref(gl), stream.cuda_stream)
+        N.check(rc, None, "fr_sobolev_loss_grad")
+        if rep:
+            times.append(time.perf_counter() - t0)
+    return {"config": "128^3 pair, 50 unrolled sobolev iterations, gradient w.r.t. v0 (3x128^3) and lambda, "
+                      "checkpoints every 10", "ms_forward_and_adjoint": 1000.0 * min(times),
+            "loss": loss.value, "grad_lambda": gl.value}
+
+
 def batched_vs_plain(dev, stream, n_pairs=16, reps=2):
     """One fr_register_batch over the uneven cohort against one fr_register per pair
     (a handle per pair size), same data, same iterations; checks the two agree bit
@@ -465,6 +492,10 @@ def main():
 
         # batched cohort against plain per-pair calls: 16 uneven pairs, 200 iterations each
         line["batched"] = batched_vs_plain(dev, stream)
+
+        # the differentiated registration: 128^3 pair, 50 iterations unrolled, gradient of
+        # J = SSD + 0.1 |m_K|^2 with respect to v0 and lambda, checkpoints every 10
+        line["adjoint"] = adjoint_timing(dev, stream)
 
         # CPU baseline: the oracle port on the host cores, bounded sample
         cores = os.cpu_count() or 1

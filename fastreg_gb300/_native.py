@@ -104,6 +104,11 @@ SIGNATURES = [
     ("fr_finish", C.c_int, [C.c_void_p, C.c_void_p]),
     ("fr_time_kernels", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     ("fr_warp", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fr_sobolev_loss_grad", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_float, C.c_int,
+                                       C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.POINTER(C.c_double),
+                                       C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
+    ("fr_warp_adjoint", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
     ("fr_stats_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
                                    C.c_int, C.c_float, C.POINTER(fr_stats), C.c_void_p]),
     ("fr_last_error", C.c_char_p, [C.c_void_p]),

@@ -354,6 +354,7 @@ int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev
     a.g = h->grad;
     a.damping = h->P.damping;
     a.step = h->P.step;
+    a.lambda = h->P.w_reg;
     frg::gaussian_taps(h->P.smooth_sigma, h->P.smooth_width, a.taps);
     a.radius = h->P.smooth_width / 2;
     a.max_update_norm = h->P.max_update_norm;

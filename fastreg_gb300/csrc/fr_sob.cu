@@ -87,9 +87,26 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                                                   lerpf_(f011 - f010, f001 - f000, s.b), s.a)
                                          : 0.f;
                 const float r = W - __ldg(T + i);
-                g0[i] = r * dWa;
-                g1[i] = r * dWb;
-                g2[i] = r * dWc;
+                // graph Laplacian of u = phi - x, neighbours inside the grid, order -x,+x,-y,+y,-z,+z
+                const bool ok[6] = {x > 0, x < P.X - 1, y > 0, y < P.Y - 1, z > 0, z < P.Z - 1};
+                const int off[6] = {-1, 1, -X, X, -XY, XY};
+                float lap[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float* __restrict__ Pc = c == 0 ? phi0 : (c == 1 ? phi1 : phi2);
+                    const float pc = __ldg(Pc + i);
+                    float acc = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        if (!ok[k]) continue;
+                        const float delta = (k / 2 == c) ? ((k & 1) ? 1.f : -1.f) : 0.f;
+                        acc = acc + ((pc - __ldg(Pc + i + off[k])) + delta);
+                    }
+                    lap[c] = acc;
+                }
+                g0[i] = (r * dWa) + (a.lambda * lap[0]);
+                g1[i] = (r * dWb) + (a.lambda * lap[1]);
+                g2[i] = (r * dWc) + (a.lambda * lap[2]);
                 e += (double)r * (double)r;
             }
         }

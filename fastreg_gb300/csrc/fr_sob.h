@@ -4,7 +4,9 @@
 // One iteration, per voxel x of every pair (phi = positions, m = momentum):
 //   W(x)   = S(phi(x))                         trilinear, cell floor clamped to dim-2
 //   g(x)   = (W(x) - T(x)) * dW/dphi(x)        exact derivative of the trilinear
-//                                              interpolant (0 along a clamped axis)
+//            + lambda * lap(phi - x)(x)        interpolant (0 along a clamped axis);
+//                                              lap = graph Laplacian over the grid's
+//                                              neighbours, lambda = W_REG
 //   gs     = G_sigma * g                       separable Gaussian, SMOOTH_WIDTH taps,
 //                                              normalised, replicate boundary, each tap
 //                                              a fused multiply-add in the order -R..R
@@ -36,6 +38,7 @@ struct SobIterArgs {
     float* m;     // momentum (3 planes)
     float* g;     // gradient (3 planes)
     float damping, step;
+    float lambda;  // weight of the displacement's graph Laplacian (W_REG)
     float taps[kMaxSmoothWidth];
     int radius;
     float max_update_norm;

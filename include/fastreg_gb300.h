@@ -146,6 +146,24 @@ int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *st
 int fr_warp(const float *d_pos, const float *d_img, const int16_t *d_lab, const int dims[3], float *d_out,
             int16_t *d_out_lab, void *stream);
 
+/* ---- the differentiated sobolev registration (no counterpart in the reference) ----
+ * J(v0, lambda) = 0.5 * sum (S(phi_K) - T)^2 + 0.1 * sum |m_K|^2 after `iters` sobolev
+ * iterations (damping, step, smooth_sigma, smooth_width as the SOLVER=sobolev keys) from
+ * phi_0 = identity and momentum m_0 = d_v0 (3 planes of N), with the displacement
+ * regulariser weighted by lambda (W_REG).  Writes J to *loss and, when d_grad_v0 is not
+ * NULL, dJ/dv0 (3 planes, device) and dJ/dlambda to *grad_lambda, by hand-written
+ * adjoint kernels with the forward states checkpointed every `checkpoint_every`
+ * iterations.  d_T, d_S: target and source (N floats each).  Synchronises `stream`. */
+int fr_sobolev_loss_grad(const float *d_T, const float *d_S, const int dims[3], const float *d_v0, float lambda,
+                         int iters, int checkpoint_every, float damping, float step, float smooth_sigma,
+                         int smooth_width, double *loss, float *d_grad_v0, double *grad_lambda, void *stream);
+
+/* adjoint of the warp W = img(pos) (trilinear, floor clamped to dim-2): d_pos_bar = wbar *
+ * d img/d pos (3 planes; 0 along an axis where pos was clamped), d_img_bar = scatter-add of
+ * the trilinear weights times wbar (N floats, zeroed first).  Either output may be NULL. */
+int fr_warp_adjoint(const float *d_pos, const float *d_img, const float *d_wbar, const int dims[3], float *d_pos_bar,
+                    float *d_img_bar, void *stream);
+
 /* ---- statistics without device allocation ----
  * No counterpart in the reference.  For callers that cannot call cudaMalloc when they
  * need the statistics of a registration (a process whose device memory belongs to

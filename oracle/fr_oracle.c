@@ -645,8 +645,28 @@ static inline void sob_locate_(const fro_dims *d, real px, real py, real pz, fro
     s->base = lin(d, gx, gy, gz);
 }
 
-/* g = (W - T) * dW/dphi with W = S(phi) trilinear; returns 0.5 * sum (W - T)^2 */
-double FN(sob_grad)(const int *dims, const real *S, const real *T, const real *phi, real *g, real *W_out) {
+/* Graph Laplacian of the displacement u = phi - x over the grid's neighbours (the
+ * gradient of 0.5 * sum over grid edges |u(x) - u(q)|^2): for each neighbour q inside the
+ * grid, in the order -x, +x, -y, +y, -z, +z, lap_c += (phi_c(x) - phi_c(q)) + (q - x)_c. */
+static inline void lap_u_(const fro_dims *d, const real *phi, int x, int y, int z, real out[3]) {
+    const int64_t N = nvox(d), i = lin(d, x, y, z);
+    const int64_t X = d->X, XY = (int64_t)d->X * d->Y;
+    const int ok[6] = {x > 0, x < d->X - 1, y > 0, y < d->Y - 1, z > 0, z < d->Z - 1};
+    const int64_t off[6] = {-1, 1, -X, X, -XY, XY};
+    for (int c = 0; c < 3; ++c) {
+        real acc = R(0);
+        for (int k = 0; k < 6; ++k) {
+            if (!ok[k]) continue;
+            const real delta = (k / 2 == c) ? ((k & 1) ? R(1) : R(-1)) : R(0);
+            acc = acc + ((phi[c * N + i] - phi[c * N + i + off[k]]) + delta);
+        }
+        out[c] = acc;
+    }
+}
+
+/* g = (W - T) * dW/dphi + lambda * lap(u) with W = S(phi) trilinear; returns 0.5 * sum (W - T)^2 */
+double FN(sob_grad)(const int *dims, const real *S, const real *T, const real *phi, real lambda, real *g,
+                    real *W_out) {
     fro_dims d = {dims[0], dims[1], dims[2]};
     const int64_t N = nvox(&d), X = d.X, XY = (int64_t)d.X * d.Y;
     double e = 0.0;
@@ -665,9 +685,12 @@ double FN(sob_grad)(const int *dims, const real *S, const real *T, const real *p
         const real dWc = s.in_z ? lerp_(lerp_(f111 - f110, f101 - f100, s.b), lerp_(f011 - f010, f001 - f000, s.b), s.a)
                                 : R(0);
         const real r = W - T[i];
-        g[i] = r * dWa;
-        g[N + i] = r * dWb;
-        g[2 * N + i] = r * dWc;
+        const int z = (int)(i / XY), y = (int)((i - z * XY) / X), x = (int)(i - z * XY - y * X);
+        real lap[3];
+        lap_u_(&d, phi, x, y, z, lap);
+        g[i] = (r * dWa) + (lambda * lap[0]);
+        g[N + i] = (r * dWb) + (lambda * lap[1]);
+        g[2 * N + i] = (r * dWc) + (lambda * lap[2]);
         if (W_out) W_out[i] = W;
         e += (double)r * (double)r;
     }
@@ -737,6 +760,7 @@ typedef struct {
     real max_update_norm;
     real damping, step, sigma;
     int width;
+    real lambda; /* W_REG: weight of the displacement's graph Laplacian */
 } fro_sob_params;
 
 /* full sobolev registration from phi = identity, m = 0; returns iterations run */
@@ -761,7 +785,7 @@ int FN(sob_register)(const int *dims, const fro_sob_params *P, const real *T, co
     int ran = 0;
     *converged = 0;
     for (int it = 1; it <= P->max_iter; ++it) {
-        double e = FN(sob_grad)(dims, S, T, phi, g, NULL);
+        double e = FN(sob_grad)(dims, S, T, phi, P->lambda, g, NULL);
         if (trace_energy) trace_energy[it - 1] = e;
         FN(sob_smooth)(dims, taps, Rr, 0, g, tmp, 0, R(0), R(0));
         FN(sob_smooth)(dims, taps, Rr, 1, tmp, g, 0, R(0), R(0));
@@ -795,5 +819,235 @@ void FN(warp_nearest_label)(const int *dims, const real *pos, const int16_t *lab
         if (iy > d.Y - 1) iy = d.Y - 1;
         if (iz > d.Z - 1) iz = d.Z - 1;
         out_lab[i] = lab[lin(&d, ix, iy, iz)];
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* Differentiated sobolev registration (the adjoint of the loop above)        */
+/* ------------------------------------------------------------------------- */
+
+/* trilinear weights of the 8 corners (order 000,100,010,110,001,101,011,111 by
+ * (dx,dy,dz)), value, position derivative (masked on clamped axes) and Hessian */
+typedef struct {
+    real w[8];
+    int64_t off[8];
+    real val, d[3], H[3][3];
+} fro_tri;
+
+static void tri_eval_(const fro_dims *d, const real *F, const fro_scell *s, fro_tri *t, int want_hessian) {
+    const int64_t X = d->X, XY = (int64_t)d->X * d->Y, b = s->base;
+    const int64_t off[8] = {0, 1, X, 1 + X, XY, 1 + XY, X + XY, 1 + X + XY};
+    real f[8];
+    for (int q = 0; q < 8; ++q) {
+        t->off[q] = b + off[q];
+        f[q] = F ? F[b + off[q]] : R(0);
+    }
+    const real a = s->a, bb = s->b, c = s->c;
+    for (int q = 0; q < 8; ++q) {
+        const real wx = (q & 1) ? a : R(1) - a, wy = (q & 2) ? bb : R(1) - bb, wz = (q & 4) ? c : R(1) - c;
+        t->w[q] = wx * wy * wz;
+    }
+    if (!F) return;
+    const real f000 = f[0], f100 = f[1], f010 = f[2], f110 = f[3], f001 = f[4], f101 = f[5], f011 = f[6], f111 = f[7];
+    const real e11 = lerp_(f111, f110, c), e10 = lerp_(f101, f100, c);
+    const real e01 = lerp_(f011, f010, c), e00 = lerp_(f001, f000, c);
+    const real A1 = lerp_(e11, e10, bb), A0 = lerp_(e01, e00, bb);
+    t->val = lerp_(A1, A0, a);
+    const real d11 = f111 - f110, d10 = f101 - f100, d01 = f011 - f010, d00 = f001 - f000;
+    t->d[0] = s->in_x ? A1 - A0 : R(0);
+    t->d[1] = s->in_y ? lerp_(e11 - e10, e01 - e00, a) : R(0);
+    t->d[2] = s->in_z ? lerp_(lerp_(d11, d10, bb), lerp_(d01, d00, bb), a) : R(0);
+    if (!want_hessian) return;
+    const int in[3] = {s->in_x, s->in_y, s->in_z};
+    real H01 = (e11 - e10) - (e01 - e00);
+    real H02 = lerp_(d11, d10, bb) - lerp_(d01, d00, bb);
+    real H12 = lerp_(d11 - d10, d01 - d00, a);
+    memset(t->H, 0, sizeof(t->H));
+    if (in[0] && in[1]) t->H[0][1] = t->H[1][0] = H01;
+    if (in[0] && in[2]) t->H[0][2] = t->H[2][0] = H02;
+    if (in[1] && in[2]) t->H[1][2] = t->H[2][1] = H12;
+}
+
+/* out(x) = sum_k w_k in(clamp(x + k)) along axis: transpose, scatter form */
+static void smooth_t_(const fro_dims *d, const real *taps, int Rr, int axis, const real *src, real *dst) {
+    const int64_t N = nvox(d);
+    const int dim = axis == 0 ? d->X : (axis == 1 ? d->Y : d->Z);
+    const int64_t stride = axis == 0 ? 1 : (axis == 1 ? (int64_t)d->X : (int64_t)d->X * d->Y);
+    memset(dst, 0, sizeof(real) * 3 * N);
+    for (int z = 0; z < d->Z; ++z)
+        for (int y = 0; y < d->Y; ++y)
+            for (int x = 0; x < d->X; ++x) {
+                const int64_t i = lin(d, x, y, z);
+                const int pos = axis == 0 ? x : (axis == 1 ? y : z);
+                for (int k = -Rr; k <= Rr; ++k) {
+                    int q = pos + k;
+                    if (q < 0) q = 0;
+                    if (q > dim - 1) q = dim - 1;
+                    const int64_t j = i + (int64_t)(q - pos) * stride;
+                    for (int c = 0; c < 3; ++c) dst[c * N + j] += taps[k + Rr] * src[c * N + i];
+                }
+            }
+}
+
+typedef struct {
+    int iters;
+    real damping, step, sigma;
+    int width;
+} fro_sobgrad_params;
+
+/* J = 0.5 sum (S(phi_K) - T)^2 + 0.1 sum |m_K|^2 after K sobolev iterations from
+ * phi_0 = identity, m_0 = v0, with regulariser weight lambda.  Returns J; with
+ * grad_v0 != NULL also dJ/dv0 (3N) and dJ/dlambda (reverse mode, all states kept). */
+double FN(sob_loss_grad)(const int *dims, const fro_sobgrad_params *P, const real *T, const real *S, const real *v0,
+                         real lambda, real *grad_v0, double *grad_lambda) {
+    fro_dims d = {dims[0], dims[1], dims[2]};
+    const int64_t N = nvox(&d), N3 = 3 * N;
+    const int K = P->iters, Rr = P->width / 2;
+    real taps[64];
+    FN(gaussian_taps)(P->sigma, P->width, taps);
+    /* every state is kept for the reverse sweep; the loss alone needs two */
+    const int keep = grad_v0 ? K + 1 : 2;
+    real *phis = (real *)malloc(sizeof(real) * N3 * keep);
+    real *ms = (real *)malloc(sizeof(real) * N3 * keep);
+    real *g = (real *)malloc(sizeof(real) * N3), *tmp = (real *)malloc(sizeof(real) * N3);
+    for (int z = 0; z < d.Z; ++z)
+        for (int y = 0; y < d.Y; ++y)
+            for (int x = 0; x < d.X; ++x) {
+                int64_t i = lin(&d, x, y, z);
+                phis[i] = (real)x;
+                phis[N + i] = (real)y;
+                phis[2 * N + i] = (real)z;
+            }
+    memcpy(ms, v0, sizeof(real) * N3);
+    for (int k = 0; k < K; ++k) {
+        const int slot = grad_v0 ? k : 0;
+        real *phi = phis + (int64_t)slot * N3, *m = ms + (int64_t)slot * N3;
+        real *phin = phi + N3, *mn = m + N3;
+        FN(sob_grad)(dims, S, T, phi, lambda, g, NULL);
+        memcpy(mn, m, sizeof(real) * N3);
+        FN(sob_smooth)(dims, taps, Rr, 0, g, tmp, 0, R(0), R(0));
+        FN(sob_smooth)(dims, taps, Rr, 1, tmp, g, 0, R(0), R(0));
+        FN(sob_smooth)(dims, taps, Rr, 2, g, mn, 1, P->damping, P->step);
+        memcpy(phin, phi, sizeof(real) * N3);
+        real mx;
+        int64_t am;
+        FN(sob_pass_b)(dims, mn, phin, &mx, &am);
+        if (!grad_v0) {
+            memcpy(phi, phin, sizeof(real) * N3);
+            memcpy(m, mn, sizeof(real) * N3);
+        }
+    }
+    const int last = grad_v0 ? K : 0;
+    const real *phiK = phis + (int64_t)last * N3, *mK = ms + (int64_t)last * N3;
+    double J = 0.0;
+    real *pbar = grad_v0 ? (real *)calloc(N3, sizeof(real)) : NULL;
+    for (int64_t i = 0; i < N; ++i) {
+        fro_scell s;
+        sob_locate_(&d, phiK[i], phiK[N + i], phiK[2 * N + i], &s);
+        fro_tri t;
+        tri_eval_(&d, S, &s, &t, 0);
+        const real r = t.val - T[i];
+        J += 0.5 * (double)r * (double)r;
+        if (pbar)
+            for (int j = 0; j < 3; ++j) pbar[j * N + i] = r * t.d[j];
+    }
+    for (int64_t i = 0; i < N3; ++i) J += 0.1 * (double)mK[i] * (double)mK[i];
+    if (!grad_v0) {
+        free(phis); free(ms); free(g); free(tmp);
+        return J;
+    }
+    real *mbar = (real *)malloc(sizeof(real) * N3);
+    for (int64_t i = 0; i < N3; ++i) mbar[i] = R(0.2) * mK[i];
+    real *pbar_k = (real *)malloc(sizeof(real) * N3);
+    real *gbar = (real *)malloc(sizeof(real) * N3);
+    double lbar = 0.0;
+    for (int k = K - 1; k >= 0; --k) {
+        const real *phi = phis + (int64_t)k * N3, *mn = ms + (int64_t)(k + 1) * N3;
+        /* phi_{k+1} = phi_k + m_{k+1}(phi_k) */
+        memcpy(pbar_k, pbar, sizeof(real) * N3);
+        for (int64_t i = 0; i < N; ++i) {
+            fro_scell s;
+            sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
+            for (int c = 0; c < 3; ++c) {
+                fro_tri t;
+                tri_eval_(&d, mn + c * N, &s, &t, 0);
+                const real pb = pbar[c * N + i];
+                for (int j = 0; j < 3; ++j) pbar_k[j * N + i] += pb * t.d[j];
+                for (int q = 0; q < 8; ++q) mbar[c * N + t.off[q]] += t.w[q] * pb;
+            }
+        }
+        /* m_{k+1} = damping * m_k - step * gs */
+        for (int64_t i = 0; i < N3; ++i) {
+            g[i] = -P->step * mbar[i];
+            mbar[i] = P->damping * mbar[i];
+        }
+        /* gs = Gz Gy Gx g  ->  gbar = Gx^T Gy^T Gz^T gsbar */
+        smooth_t_(&d, taps, Rr, 2, g, tmp);
+        smooth_t_(&d, taps, Rr, 1, tmp, g);
+        smooth_t_(&d, taps, Rr, 0, g, gbar);
+        /* g = r dW + lambda lap(u) */
+        for (int z = 0; z < d.Z; ++z)
+            for (int y = 0; y < d.Y; ++y)
+                for (int x = 0; x < d.X; ++x) {
+                    const int64_t i = lin(&d, x, y, z);
+                    real lap[3];
+                    lap_u_(&d, phi, x, y, z, lap);
+                    for (int c = 0; c < 3; ++c) lbar += (double)gbar[c * N + i] * (double)lap[c];
+                    /* Laplacian part: graph Laplacian is symmetric */
+                    const int64_t X = d.X, XY = (int64_t)d.X * d.Y;
+                    const int ok[6] = {x > 0, x < d.X - 1, y > 0, y < d.Y - 1, z > 0, z < d.Z - 1};
+                    const int64_t off[6] = {-1, 1, -X, X, -XY, XY};
+                    for (int c = 0; c < 3; ++c)
+                        for (int kk = 0; kk < 6; ++kk)
+                            if (ok[kk]) pbar_k[c * N + i] += lambda * (gbar[c * N + i] - gbar[c * N + i + off[kk]]);
+                    /* data part: d/dphi of (S(phi) - T) dS(phi) */
+                    fro_scell s;
+                    sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
+                    fro_tri t;
+                    tri_eval_(&d, S, &s, &t, 1);
+                    const real r = t.val - T[i];
+                    real gd = R(0);
+                    for (int c = 0; c < 3; ++c) gd += gbar[c * N + i] * t.d[c];
+                    for (int j = 0; j < 3; ++j) {
+                        real h = R(0);
+                        for (int c = 0; c < 3; ++c) h += gbar[c * N + i] * t.H[c][j];
+                        pbar_k[j * N + i] += gd * t.d[j] + r * h;
+                    }
+                }
+        memcpy(pbar, pbar_k, sizeof(real) * N3);
+    }
+    memcpy(grad_v0, mbar, sizeof(real) * N3);
+    *grad_lambda = lbar;
+    free(phis); free(ms); free(g); free(tmp); free(pbar); free(mbar); free(pbar_k); free(gbar);
+    return J;
+}
+
+/* adjoint of the warp W = img(pos) (sobolev cell): pos_bar = Wbar * dimg/dpos,
+ * img_bar(corner) += weight * Wbar */
+void FN(warp_adjoint)(const int *dims, const real *pos, const real *img, const real *wbar, real *pos_bar,
+                      real *img_bar) {
+    fro_dims d = {dims[0], dims[1], dims[2]};
+    const int64_t N = nvox(&d);
+    memset(img_bar, 0, sizeof(real) * N);
+    for (int64_t i = 0; i < N; ++i) {
+        fro_scell s;
+        sob_locate_(&d, pos[i], pos[N + i], pos[2 * N + i], &s);
+        fro_tri t;
+        tri_eval_(&d, img, &s, &t, 0);
+        for (int j = 0; j < 3; ++j) pos_bar[j * N + i] = wbar[i] * t.d[j];
+        for (int q = 0; q < 8; ++q) img_bar[t.off[q]] += t.w[q] * wbar[i];
+    }
+}
+
+/* the warp with the sobolev cell (value only), for finite differences of the adjoint */
+void FN(warp_sob)(const int *dims, const real *pos, const real *img, real *out) {
+    fro_dims d = {dims[0], dims[1], dims[2]};
+    const int64_t N = nvox(&d);
+    for (int64_t i = 0; i < N; ++i) {
+        fro_scell s;
+        sob_locate_(&d, pos[i], pos[N + i], pos[2 * N + i], &s);
+        fro_tri t;
+        tri_eval_(&d, img, &s, &t, 0);
+        out[i] = t.val;
     }
 }

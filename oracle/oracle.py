@@ -36,12 +36,19 @@ def _ref_params_type(real):
 def _sob_params_type(real):
     class SobParams(C.Structure):
         _fields_ = [("max_iter", C.c_int), ("max_update_norm", real), ("damping", real), ("step", real),
-                    ("sigma", real), ("width", C.c_int)]
+                    ("sigma", real), ("width", C.c_int), ("lam", real)]
     return SobParams
+
+
+def _sobgrad_params_type(real):
+    class SobGradParams(C.Structure):
+        _fields_ = [("iters", C.c_int), ("damping", real), ("step", real), ("sigma", real), ("width", C.c_int)]
+    return SobGradParams
 
 
 RefParams32, RefParams64 = _ref_params_type(C.c_float), _ref_params_type(C.c_double)
 SobParams32, SobParams64 = _sob_params_type(C.c_float), _sob_params_type(C.c_double)
+SobGradParams32, SobGradParams64 = _sobgrad_params_type(C.c_float), _sobgrad_params_type(C.c_double)
 
 
 class Stats(C.Structure):
@@ -208,13 +215,15 @@ def gaussian_taps(sigma, width, prec=32):
     return out
 
 
-def sob_grad(S, T, phi, prec=32):
+def sob_grad(S, T, phi, lam=0.0, prec=32):
     S, T, phi = _f(S, prec), _f(T, prec), _f(phi, prec)
     g = np.empty_like(phi)
     W = np.empty_like(S)
+    real = C.c_float if prec == 32 else C.c_double
     fn = getattr(lib(prec), f"fro{prec}_sob_grad")
     fn.restype = C.c_double
-    e = fn(_dims(S.shape), _p(S), _p(T), _p(phi), _p(g), _p(W))
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, real, C.c_void_p, C.c_void_p]
+    e = fn(_dims(S.shape), _p(S), _p(T), _p(phi), lam, _p(g), _p(W))
     return g, float(e), W
 
 
@@ -251,6 +260,7 @@ def sob_register(params, T, S, prec=32):
     P.max_iter = int(params.max_iter)
     P.max_update_norm = params.max_update_norm
     P.damping, P.step, P.sigma, P.width = params.damping, params.step, params.smooth_sigma, int(params.smooth_width)
+    P.lam = params.w_reg
     z, y, x = T.shape
     dt = _dt(prec)
     phi = np.empty((3, z, y, x), dt)
@@ -264,3 +274,35 @@ def sob_register(params, T, S, prec=32):
                                                        _p(tn), _p(ti), _p(te), C.byref(conv))
     return dict(phi=phi, m=m, iterations=int(ran), converged=bool(conv.value), trace_norm=tn[:ran],
                 trace_idx=ti[:ran], trace_energy=te[:ran])
+
+
+def sob_loss_grad(params, T, S, v0, lam, iters, with_grad=True, prec=64):
+    """J = 0.5 sum (S(phi_K) - T)^2 + 0.1 sum |m_K|^2 of a K-iteration sobolev
+    registration from phi = identity, m = v0; returns (J, dJ/dv0, dJ/dlambda)."""
+    T, S, v0 = _f(T, prec), _f(S, prec), _f(v0, prec)
+    real = C.c_float if prec == 32 else C.c_double
+    P = (SobGradParams32 if prec == 32 else SobGradParams64)()
+    P.iters, P.damping, P.step, P.sigma, P.width = int(iters), params.damping, params.step, params.smooth_sigma, \
+        int(params.smooth_width)
+    fn = getattr(lib(prec), f"fro{prec}_sob_loss_grad")
+    fn.restype = C.c_double
+    fn.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, real, C.c_void_p, C.c_void_p]
+    gv = np.zeros_like(v0) if with_grad else None
+    gl = C.c_double()
+    J = fn(_dims(T.shape), C.byref(P), _p(T), _p(S), _p(v0), lam, _p(gv) if with_grad else None, C.byref(gl))
+    return float(J), gv, float(gl.value)
+
+
+def warp_adjoint(pos, img, wbar, prec=64):
+    pos, img, wbar = _f(pos, prec), _f(img, prec), _f(wbar, prec)
+    pb = np.empty_like(pos)
+    ib = np.empty_like(img)
+    getattr(lib(prec), f"fro{prec}_warp_adjoint")(_dims(img.shape), _p(pos), _p(img), _p(wbar), _p(pb), _p(ib))
+    return pb, ib
+
+
+def warp_sob(pos, img, prec=64):
+    pos, img = _f(pos, prec), _f(img, prec)
+    out = np.empty_like(img)
+    getattr(lib(prec), f"fro{prec}_warp_sob")(_dims(img.shape), _p(pos), _p(img), _p(out))
+    return out

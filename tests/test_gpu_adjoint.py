@@ -1,0 +1,132 @@
+"""The hand-written adjoint kernels on the GPU (fr_sobolev_loss_grad, fr_warp_adjoint)
+against the FP64 oracle and central finite differences of the FP64 forward.
+
+The registration is wrapped in a torch.autograd.Function here, in the test harness only:
+the library itself is plain CUDA behind the C ABI."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from fastreg_gb300 import Params, _native as N
+from oracle import oracle as O
+from tests.helpers import images, rng, smooth_noise
+
+pytestmark = pytest.mark.gpu
+
+
+def _loss_grad(T, S, v0, lam, K, ck, P, want_grad=True):
+    import torch
+    lib = N.load()
+    z, y, x = T.shape
+    dims = (C.c_int * 3)(x, y, z)
+    loss = C.c_double()
+    gl = C.c_double()
+    gv = torch.empty_like(v0) if want_grad else None
+    rc = lib.fr_sobolev_loss_grad(T.data_ptr(), S.data_ptr(), dims, v0.data_ptr(), float(lam), int(K), int(ck),
+                                  P.damping, P.step, P.smooth_sigma, int(P.smooth_width), C.byref(loss),
+                                  gv.data_ptr() if want_grad else None, C.byref(gl), None)
+    assert rc == N.FR_OK, lib.fr_last_error(None)
+    return loss.value, gv, gl.value
+
+
+def _registration_fn():
+    import torch
+
+    class SobolevRegistration(torch.autograd.Function):
+        """J(v0, lambda) of a K-iteration sobolev registration; backward runs the
+        adjoint kernels."""
+
+        @staticmethod
+        def forward(ctx, v0, lam, T, S, K, ck, P):
+            J, gv, gl = _loss_grad(T, S, v0.detach().contiguous(), float(lam), K, ck, P)
+            ctx.save_for_backward(gv, torch.tensor(gl, dtype=torch.float64))
+            return torch.tensor(J, dtype=torch.float64, device=v0.device)
+
+        @staticmethod
+        def backward(ctx, gJ):
+            gv, gl = ctx.saved_tensors
+            return (gJ.to(gv.dtype) * gv, (gJ.cpu() * gl).to(torch.float64), None, None, None, None, None)
+
+    return SobolevRegistration.apply
+
+
+def test_loss_gradient_against_fp64_oracle_and_finite_differences(cuda):
+    import torch
+    dims = (24, 20, 18)
+    d = images(dims, 21)
+    P = Params(volume_dims=dims, solver="sobolev", smooth_sigma=1.5, smooth_width=7, damping=0.9, step=0.5)
+    v0 = smooth_noise(rng(2), (3,) + dims[::-1], 0.3)
+    lam, K, ck = 0.2, 12, 5
+    T, S = (torch.from_numpy(d[k]).to(cuda) for k in ("T", "S"))
+    v0_t = torch.from_numpy(v0).to(cuda).requires_grad_(True)
+    lam_t = torch.tensor(lam, dtype=torch.float64, requires_grad=True)
+    J = _registration_fn()(v0_t, lam_t, T, S, K, ck, P)
+    J.backward()
+    gv = v0_t.grad.cpu().numpy().astype(np.float64)
+    gl = float(lam_t.grad)
+
+    J64, gv64, gl64 = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam, K)
+    J32, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0, lam, K, False, prec=32)
+    assert abs(float(J) - J32) <= 1e-9 * abs(J32)          # same FP32 forward, FP64 sums in another order
+    assert abs(float(J) - J64) <= 1e-5 * abs(J64)
+    assert abs(gl - gl64) <= 1e-4 * abs(gl64), (gl, gl64)
+    scale = float(np.abs(gv64).max())
+    err = np.abs(gv - gv64).max() / scale
+    assert err <= 1e-3, f"dJ/dv0: max |gpu - fp64| / max |grad| = {err:.3g}"
+
+    # central finite differences of the FP64 forward (eps 1e-6: below the kinks of
+    # trilinear interpolation) at 64 random voxel components and at lambda
+    eps = 1e-6
+    Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam + eps, K, False)
+    Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam - eps, K, False)
+    fd = (Jp - Jm) / (2 * eps)
+    assert abs(gl - fd) <= 1e-4 * abs(fd), (gl, fd)
+    r = rng(11)
+    bad = []
+    for _ in range(64):
+        c = int(r.integers(0, 3))
+        z, y, x = (int(r.integers(0, n)) for n in v0.shape[1:])
+        vp = v0.astype(np.float64)
+        vm = vp.copy()
+        vp[c, z, y, x] += eps
+        vm[c, z, y, x] -= eps
+        Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vp, lam, K, False)
+        Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vm, lam, K, False)
+        fdv = (Jp - Jm) / (2 * eps)
+        if abs(fdv - gv[c, z, y, x]) > 1e-4 * max(abs(fdv), 1e-2 * scale):
+            bad.append((c, z, y, x, fdv, gv[c, z, y, x]))
+    assert not bad, bad[:4]
+
+
+def test_checkpointing_does_not_change_the_gradient(cuda):
+    import torch
+    dims = (16, 14, 12)
+    d = images(dims, 4)
+    P = Params(volume_dims=dims, solver="sobolev", smooth_sigma=1.5, smooth_width=7, damping=0.9, step=0.5)
+    v0 = torch.from_numpy(smooth_noise(rng(3), (3,) + dims[::-1], 0.2)).to(cuda)
+    T, S = (torch.from_numpy(d[k]).to(cuda) for k in ("T", "S"))
+    J1, g1, l1 = _loss_grad(T, S, v0, 0.1, 10, 10, P)
+    J2, g2, l2 = _loss_grad(T, S, v0, 0.1, 10, 3, P)
+    assert J1 == J2
+    assert torch.allclose(g1, g2, rtol=1e-5, atol=1e-6 * float(g1.abs().max()))
+    assert abs(l1 - l2) <= 1e-6 * abs(l1)
+
+
+def test_warp_adjoint(cuda):
+    import torch
+    lib = N.load()
+    dims = (20, 18, 16)
+    r = rng(9)
+    img = r.normal(0, 1, dims[::-1]).astype(np.float32)
+    pos = np.stack(np.meshgrid(np.arange(16), np.arange(18), np.arange(20), indexing="ij")[::-1]).astype(np.float32)
+    pos = pos + r.uniform(-2.5, 2.5, pos.shape).astype(np.float32)
+    wbar = r.normal(0, 1, dims[::-1]).astype(np.float32)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)  # noqa: E731
+    pb, ib = torch.empty((3,) + dims[::-1], device=cuda), torch.empty(dims[::-1], device=cuda)
+    cd = (C.c_int * 3)(*dims)
+    assert lib.fr_warp_adjoint(t(pos).data_ptr(), t(img).data_ptr(), t(wbar).data_ptr(), cd, pb.data_ptr(),
+                               ib.data_ptr(), None) == N.FR_OK
+    pb64, ib64 = O.warp_adjoint(pos, img, wbar)
+    assert np.abs(pb.cpu().numpy() - pb64).max() <= 1e-5 * max(1.0, np.abs(pb64).max())
+    assert np.abs(ib.cpu().numpy() - ib64).max() <= 1e-5 * max(1.0, np.abs(ib64).max())
