@@ -68,34 +68,42 @@ def test_loss_gradient_against_fp64_oracle_and_finite_differences(cuda):
 
     J64, gv64, gl64 = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam, K)
     J32, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0, lam, K, False, prec=32)
-    assert abs(float(J) - J32) <= 1e-9 * abs(J32)          # same FP32 forward, FP64 sums in another order
-    assert abs(float(J) - J64) <= 1e-5 * abs(J64)
+    J = float(J.detach())
+    assert abs(J - J32) <= 1e-9 * abs(J32)          # same FP32 forward, FP64 sums in another order
+    assert abs(J - J64) <= 1e-5 * abs(J64)
     assert abs(gl - gl64) <= 1e-4 * abs(gl64), (gl, gl64)
     scale = float(np.abs(gv64).max())
     err = np.abs(gv - gv64).max() / scale
     assert err <= 1e-3, f"dJ/dv0: max |gpu - fp64| / max |grad| = {err:.3g}"
 
-    # central finite differences of the FP64 forward (eps 1e-6: below the kinks of
-    # trilinear interpolation) at 64 random voxel components and at lambda
-    eps = 1e-6
-    Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam + eps, K, False)
-    Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam - eps, K, False)
-    fd = (Jp - Jm) / (2 * eps)
-    assert abs(gl - fd) <= 1e-4 * abs(fd), (gl, fd)
+    # central finite differences of the FP64 forward at 64 random voxel components and at
+    # lambda.  The model is piecewise smooth (trilinear interpolation has kinks on cell
+    # faces); a difference whose step lets any of the ~1e5 sample positions cross a face
+    # measures a mix of two slopes, so each check takes the best of three small steps.
+    def fd_lambda(eps):
+        Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam + eps, K, False)
+        Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], v0.astype(np.float64), lam - eps, K, False)
+        return (Jp - Jm) / (2 * eps)
+
+    errs = [abs(gl - fd_lambda(eps)) / abs(gl) for eps in (1e-6, 1e-7, 1e-8)]
+    assert min(errs) <= 1e-4, errs
     r = rng(11)
     bad = []
     for _ in range(64):
         c = int(r.integers(0, 3))
         z, y, x = (int(r.integers(0, n)) for n in v0.shape[1:])
-        vp = v0.astype(np.float64)
-        vm = vp.copy()
-        vp[c, z, y, x] += eps
-        vm[c, z, y, x] -= eps
-        Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vp, lam, K, False)
-        Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vm, lam, K, False)
-        fdv = (Jp - Jm) / (2 * eps)
-        if abs(fdv - gv[c, z, y, x]) > 1e-4 * max(abs(fdv), 1e-2 * scale):
-            bad.append((c, z, y, x, fdv, gv[c, z, y, x]))
+        best = np.inf
+        for eps in (1e-6, 1e-7):
+            vp = v0.astype(np.float64)
+            vm = vp.copy()
+            vp[c, z, y, x] += eps
+            vm[c, z, y, x] -= eps
+            Jp, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vp, lam, K, False)
+            Jm, _, _ = O.sob_loss_grad(P, d["T"], d["S"], vm, lam, K, False)
+            fdv = (Jp - Jm) / (2 * eps)
+            best = min(best, abs(fdv - gv[c, z, y, x]) / max(abs(fdv), 1e-2 * scale))
+        if best > 1e-4:
+            bad.append((c, z, y, x, best))
     assert not bad, bad[:4]
 
 
@@ -108,7 +116,7 @@ def test_checkpointing_does_not_change_the_gradient(cuda):
     T, S = (torch.from_numpy(d[k]).to(cuda) for k in ("T", "S"))
     J1, g1, l1 = _loss_grad(T, S, v0, 0.1, 10, 10, P)
     J2, g2, l2 = _loss_grad(T, S, v0, 0.1, 10, 3, P)
-    assert J1 == J2
+    assert abs(J1 - J2) <= 1e-12 * abs(J1)  # FP64 atomics add the block sums in any order
     assert torch.allclose(g1, g2, rtol=1e-5, atol=1e-6 * float(g1.abs().max()))
     assert abs(l1 - l2) <= 1e-6 * abs(l1)
 
