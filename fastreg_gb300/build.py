@@ -62,7 +62,22 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> Path:
     os.replace(tmp, out)
     if verbose:
         print(f"built {out}")
+    build_app(verbose)
     return out
+
+
+def build_app(verbose: bool = False) -> Path:
+    """The command-line app (fastreg_gb300/app), linked against the library."""
+    src = PKG / "app" / "fastreg_app.cpp"
+    exe = LIBDIR / "fastreg_app"
+    cmd = [nvcc(), "-std=c++17", "-O2", str(src), "-o", str(exe), "-L", str(LIBDIR), "-lfastreg_gb300",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"app build failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print(f"built {exe}")
+    return exe
 
 
 if __name__ == "__main__":

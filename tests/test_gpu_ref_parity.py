@@ -201,3 +201,25 @@ def test_cuda_path_matches_reference_kernels(cuda, path):
     assert np.abs(norms.astype(np.float64) - f["trace_norm"]).max() <= 1e-6 * float(np.abs(f["trace_norm"]).max())
     assert_bitexact(vox, f["trace_idx"], "max update voxels")
     fr.close()
+
+
+def test_verbose_mode_prints_and_matches_graph_mode(cuda, capfd):
+    """verbosity 1 runs the host-driven loop with the reference's prints (energy at
+    iteration 1, every 100 and the last; max update norm; Dice) and the same bits as the
+    graph path (solver.cu:329-433)."""
+    dims = (20, 18, 16)
+    d = images(dims, 61)
+    out = {}
+    for verbosity in (0, 1):
+        P = _params(dims, max_iter=12, alpha=0.03, verbosity=verbosity)
+        fr = FastReg(P)
+        bufs = [_to(cuda, d[k]) for k in ("T", "labT", "S", "labS")]
+        fr(*bufs)
+        out[verbosity] = (fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), bufs[2].cpu().numpy(), fr.stats())
+        fr.close()
+    text = capfd.readouterr().out
+    assert "iter. no. 1" in text and "data energy + w_reg * reg energy" in text
+    assert "max. update norm" in text and "DICE COEFFICIENT" in text
+    assert_bitexact(out[1][0], out[0][0], "psi (verbose vs graph)")
+    assert_bitexact(out[1][1], out[0][1], "S o psi (verbose vs graph)")
+    assert out[1][2].e_data == out[0][2].e_data
