@@ -518,6 +518,7 @@ int run_registration(fr_handle* h, cudaStream_t s) {
             return FR_OK;
         }
         if (iter == P.max_iter) printf("SOLVER REACHED MAX. NO. OF ITERATIONS WITHOUT CONVERGING\n");
+        fflush(stdout);
     }
     return FR_OK;
 }
@@ -859,6 +860,7 @@ int fr_register_batch(fr_handle* h, const fr_pair* pairs, int n_pairs, void* str
             for (int l = 1; l < h->P.no_labels; ++l) printf("label %d: %g\n", l, st.dice[l]);
             printf("all labels: %g\n", st.dice_all);
         }
+        fflush(stdout);
     }
     return rc;
 }
