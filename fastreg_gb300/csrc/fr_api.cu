@@ -114,6 +114,19 @@ int fail(fr_handle* h, int code, const char* fmt, ...) {
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// an index of the packed (row-padded) layout -> the caller's x + X*(y + Y*z)
+long long user_index(const Pair& P, long long ip) {
+    const long long row = ip / P.Xp, x = ip - row * P.Xp;
+    return x + (long long)P.X * row;
+}
+
+// decode a max-norm key: norm and packed index (index 0 when the norm is 0)
+void decode_key(unsigned long long k, float* norm, long long* ip) {
+    const unsigned bits = (unsigned)(k >> 32);
+    std::memcpy(norm, &bits, 4);
+    *ip = bits ? (long long)(0xffffffffu - (unsigned)(k & 0xffffffffu)) : 0;
+}
+
 // t for every iteration: t = alpha, then t += alpha with the RESET_ITER restart
 // (solver.cu:327-328,428-432)
 std::vector<float> t_schedule(const fr_params& P) {
@@ -179,8 +192,9 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
                             pairs[p].dims[c]);
             dims[p][c] = pairs[p].dims[c];
         }
-        long long N = (long long)dims[p][0] * dims[p][1] * dims[p][2];
-        if (N > 0xfffffffeLL) return fail(h, FR_ERR_INVALID_ARG, "pair %d has %lld voxels (limit 2^32-2)", p, N);
+        const long long Np = (long long)((dims[p][0] + 3) / 4 * 4) * dims[p][1] * dims[p][2];
+        if (Np > 0x7fffffffLL)
+            return fail(h, FR_ERR_INVALID_ARG, "pair %d is too large (%lld padded voxels, limit 2^31-1)", p, Np);
     }
     const int want_trace = std::max(h->P.max_iter, 1);
     if (h->block && dims == h->dims && h->trace_cap >= want_trace) return FR_OK;
@@ -196,7 +210,8 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         P.X = dims[p][0];
         P.Y = dims[p][1];
         P.Z = dims[p][2];
-        P.N = (long long)P.X * P.Y * P.Z;
+        P.Xp = (P.X + 3) / 4 * 4;  // rows on 16-byte boundaries
+        P.N = (long long)P.Xp * P.Y * P.Z;
         P.off = off;
         off += (long long)align_up((size_t)P.N, 32);
         const int tz = h->P.solver == FR_SOLVER_SOBOLEV ? frg::kSobTileZ : frg::kTileZ;
@@ -500,11 +515,11 @@ int run_registration(fr_handle* h, cudaStream_t s) {
         FR_CUDA(h, cudaMemcpyAsync(stop.data(), h->stop, sizeof(int) * h->npairs, cudaMemcpyDeviceToHost, s));
         FR_CUDA(h, cudaStreamSynchronize(s));
         if (report) {
-            unsigned bits = (unsigned)(k[0] >> 32);
             float mx;
-            std::memcpy(&mx, &bits, 4);
-            long long idx = bits ? (long long)(0xffffffffu - (unsigned)(k[0] & 0xffffffffu)) : 0;
+            long long ip;
+            decode_key(k[0], &mx, &ip);
             const Pair& P0 = h->hpairs[0];
+            const long long idx = user_index(P0, ip);
             long long zz = idx / ((long long)P0.X * P0.Y);
             long long yy = (idx - zz * P0.X * P0.Y) / P0.X;
             long long xx = idx - P0.X * (yy + (long long)P0.Y * zz);
@@ -588,10 +603,9 @@ int host_stats(fr_handle* h) {
         st.converged = stop[p] != 0;
         st.iterations = stop[p] ? stop[p] : h->last_iter;
         if (st.iterations > 0) {
-            unsigned long long k = trace[(size_t)(st.iterations - 1) * n + p];
-            unsigned bits = (unsigned)(k >> 32);
-            std::memcpy(&st.last_max_update_norm, &bits, 4);
-            st.last_max_update_voxel = bits ? (int64_t)(0xffffffffu - (unsigned)(k & 0xffffffffu)) : 0;
+            long long ip;
+            decode_key(trace[(size_t)(st.iterations - 1) * n + p], &st.last_max_update_norm, &ip);
+            st.last_max_update_voxel = (int64_t)user_index(h->hpairs[p], ip);
         }
         st.e_data = energy[2 * p];
         st.e_reg = energy[2 * p + 1];
@@ -900,10 +914,11 @@ int fr_get_trace(fr_handle* h, int pair, float* norms, int64_t* voxels, int cap,
     FR_CUDA(h, cudaMemcpy(tr.data(), h->trace, sizeof(unsigned long long) * tr.size(), cudaMemcpyDeviceToHost));
     const int m = std::min(n, cap);
     for (int i = 0; i < m; ++i) {
-        unsigned long long k = tr[(size_t)i * h->npairs + pair];
-        unsigned bits = (unsigned)(k >> 32);
-        if (norms) std::memcpy(norms + i, &bits, 4);
-        if (voxels) voxels[i] = bits ? (int64_t)(0xffffffffu - (unsigned)(k & 0xffffffffu)) : 0;
+        float nrm;
+        long long ip;
+        decode_key(tr[(size_t)i * h->npairs + pair], &nrm, &ip);
+        if (norms) norms[i] = nrm;
+        if (voxels) voxels[i] = (int64_t)user_index(h->hpairs[pair], ip);
     }
     if (n_out) *n_out = n;
     return FR_OK;
@@ -959,9 +974,11 @@ int fr_get_field(fr_handle* h, int pair, int which, float* d_buf, void* stream) 
         sel = (stop ? stop : h->last_iter) & 1;
     }
     const Pair& P = h->hpairs[pair];
+    const size_t nu = (size_t)P.X * P.Y * P.Z;  // caller's (unpadded) plane
     for (int c = 0; c < ncomp; ++c)
-        FR_CUDA(h, cudaMemcpyAsync(d_buf + c * P.N, bufs[sel] + c * h->NT + P.off, sizeof(float) * P.N,
-                                   cudaMemcpyDeviceToDevice, s));
+        FR_CUDA(h, cudaMemcpy2DAsync(d_buf + c * nu, sizeof(float) * P.X, bufs[sel] + c * h->NT + P.off,
+                                     sizeof(float) * P.Xp, sizeof(float) * P.X, (size_t)P.Y * P.Z,
+                                     cudaMemcpyDeviceToDevice, s));
     return FR_OK;
 }
 
@@ -973,10 +990,12 @@ int fr_set_field(fr_handle* h, int pair, int which, const float* d_buf, void* st
     if (rc != FR_OK) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     const Pair& P = h->hpairs[pair];
+    const size_t nu = (size_t)P.X * P.Y * P.Z;  // caller's (unpadded) plane
     for (int b = 0; b < nbufs; ++b)
         for (int c = 0; c < ncomp; ++c)
-            FR_CUDA(h, cudaMemcpyAsync(bufs[b] + c * h->NT + P.off, d_buf + c * P.N, sizeof(float) * P.N,
-                                       cudaMemcpyDeviceToDevice, s));
+            FR_CUDA(h, cudaMemcpy2DAsync(bufs[b] + c * h->NT + P.off, sizeof(float) * P.Xp, d_buf + c * nu,
+                                         sizeof(float) * P.X, sizeof(float) * P.X, (size_t)P.Y * P.Z,
+                                         cudaMemcpyDeviceToDevice, s));
     h->stats_ready = false;
     return FR_OK;
 }
@@ -1032,6 +1051,7 @@ int fr_warp(const float* d_pos, const float* d_img, const int16_t* d_lab, const 
     P.X = dims[0];
     P.Y = dims[1];
     P.Z = dims[2];
+    P.Xp = P.X;  // the caller's unpadded layout
     P.N = (long long)P.X * P.Y * P.Z;
     P.off = 0;
     int dev = 0, sms = 0, per_sm = 0;

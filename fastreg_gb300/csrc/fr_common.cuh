@@ -1,10 +1,12 @@
 // fr_common.cuh -- shared device-side types and helpers of the fastreg GB300 kernels.
 //
 // Layout in HBM (all pairs of a cohort packed into one allocation per field):
-//   scalar field  f[off_p + i]                    i = x + X*(y + Y*z), x fastest
+//   scalar field  f[off_p + i]                    i = x + Xp*(y + Y*z), x fastest
 //   vector field  f[c*NT + off_p + i], c = 0,1,2  three planes (SoA), NT = packed voxels
-// off_p is the voxel offset of pair p, rounded up to 32 voxels (128 B) so that every
-// x-row of every pair starts a coalesced segment when X is a multiple of 32.
+// Xp is X rounded up to a multiple of 4 (rows start on 16-byte boundaries); the pad
+// columns are zero and never written.  off_p, the voxel offset of pair p, is a
+// multiple of 32 (128 B).  The caller's buffers keep the reference's unpadded layout
+// x + X*(y + Y*z); pack_init_kernel and finalize_kernel convert.
 //
 // Arithmetic contract (mirrored by the CPU oracle): the library is compiled with
 // --fmad=false, so a*b+c is never contracted; the only fused multiply-adds are the
@@ -18,9 +20,10 @@ namespace frg {
 
 // One registration pair inside a packed cohort.
 struct Pair {
-    int X, Y, Z, pad;
+    int X, Y, Z;
+    int Xp;         // row pitch in the packed arrays (X rounded up to a multiple of 4)
     long long off;  // voxel offset into the packed arrays
-    long long N;    // X*Y*Z
+    long long N;    // Xp*Y*Z: the pair's extent in the packed arrays
 };
 
 // A tile of work: pair index and the tile origin (x0, y0, z0).
@@ -31,6 +34,11 @@ constexpr int kTileY = 8;   // rows per block
 constexpr int kTileZ = 16;  // slices marched by each thread
 
 __device__ __forceinline__ long long lin(const Pair& P, int x, int y, int z) {
+    return (long long)x + (long long)P.Xp * ((long long)y + (long long)P.Y * z);
+}
+
+// index of (x, y, z) in the caller's unpadded layout
+__device__ __forceinline__ long long user_lin(const Pair& P, int x, int y, int z) {
     return (long long)x + (long long)P.X * ((long long)y + (long long)P.Y * z);
 }
 
@@ -65,7 +73,7 @@ __device__ __forceinline__ Cell locate(const Pair& P, float px, float py, float 
 // to the next row/slice (weight 0 there); an index past the last voxel is clamped.
 // F points at the pair's plane (already offset by off_p).
 __device__ __forceinline__ float tri_unchecked(const float* __restrict__ F, const Pair& P, const Cell& cl) {
-    const long long X = P.X, XY = (long long)P.X * P.Y, last = P.N - 1;
+    const long long X = P.Xp, XY = (long long)P.Xp * P.Y, last = P.N - 1;
     const long long b = cl.base;
     auto at = [&](long long d) -> float {
         long long j = b + d;
@@ -80,7 +88,7 @@ __device__ __forceinline__ float tri_unchecked(const float* __restrict__ F, cons
 // Trilinear sample with get_global_idx addressing (include/cuda/cuda_utils.hpp:31-37,
 // 109-136): a corner outside the grid reads element 0 of the field.
 __device__ __forceinline__ float tri_checked(const float* __restrict__ F, const Pair& P, const Cell& cl) {
-    const long long X = P.X, XY = (long long)P.X * P.Y;
+    const long long X = P.Xp, XY = (long long)P.Xp * P.Y;
     const long long b = cl.base;
     const bool ox = cl.gx + 1 < P.X, oy = cl.gy + 1 < P.Y, oz = cl.gz + 1 < P.Z;
     const float f0 = __ldg(F);
@@ -104,7 +112,8 @@ struct Cell32 {
     float a, b, c;
 };
 
-__device__ __forceinline__ Cell32 locate32(int X, int Y, int Z, float px, float py, float pz) {
+// X, Y, Z: grid extents; Xp: row pitch of the array the cell indexes
+__device__ __forceinline__ Cell32 locate32(int X, int Y, int Z, int Xp, float px, float py, float pz) {
     Cell32 cl;
     const float cx = fminf(fmaxf(0.f, px), (float)(X - 1));
     const float cy = fminf(fmaxf(0.f, py), (float)(Y - 1));
@@ -115,7 +124,7 @@ __device__ __forceinline__ Cell32 locate32(int X, int Y, int Z, float px, float 
     cl.a = cx - (float)cl.gx;
     cl.b = cy - (float)cl.gy;
     cl.c = cz - (float)cl.gz;
-    cl.base = cl.gx + X * (cl.gy + Y * cl.gz);
+    cl.base = cl.gx + Xp * (cl.gy + Y * cl.gz);
     return cl;
 }
 
@@ -126,7 +135,8 @@ __device__ __forceinline__ float trilerp(float f111, float f110, float f101, flo
 }
 
 // tri_unchecked with 32-bit indices: corners past the last voxel (only possible when
-// the cell touches the end of the array) are clamped on a slow path.
+// the cell touches the end of the array) are clamped on a slow path.  X, XY, N are the
+// strides and extent of the array (pitched for the packed arrays).
 __device__ __forceinline__ float tri_unchecked32(const float* __restrict__ F, int X, int XY, int N, const Cell32& cl) {
     const int b = cl.base;
     if (b + 1 + X + XY <= N - 1) {
@@ -139,20 +149,22 @@ __device__ __forceinline__ float tri_unchecked32(const float* __restrict__ F, in
                    __ldg(F + min(b + X, last)), __ldg(F + min(b + XY, last)), __ldg(F + b), cl.a, cl.b, cl.c);
 }
 
-// tri_checked with 32-bit indices: corners outside the grid read element 0.
-__device__ __forceinline__ float tri_checked32(const float* __restrict__ F, int X, int Y, int Z, int XY,
+// tri_checked with 32-bit indices: corners outside the grid read element 0.  X, Y, Z:
+// grid extents; Xp, XYp: strides of the array.
+__device__ __forceinline__ float tri_checked32(const float* __restrict__ F, int X, int Y, int Z, int Xp, int XYp,
                                                const Cell32& cl) {
     const int b = cl.base;
     const bool ox = cl.gx + 1 < X, oy = cl.gy + 1 < Y, oz = cl.gz + 1 < Z;
     if (ox && oy && oz) {
-        return trilerp(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), __ldg(F + b + 1 + XY), __ldg(F + b + 1),
-                       __ldg(F + b + X + XY), __ldg(F + b + X), __ldg(F + b + XY), __ldg(F + b), cl.a, cl.b, cl.c);
+        return trilerp(__ldg(F + b + 1 + Xp + XYp), __ldg(F + b + 1 + Xp), __ldg(F + b + 1 + XYp), __ldg(F + b + 1),
+                       __ldg(F + b + Xp + XYp), __ldg(F + b + Xp), __ldg(F + b + XYp), __ldg(F + b), cl.a, cl.b,
+                       cl.c);
     }
     const float f0 = __ldg(F);
-    return trilerp((ox && oy && oz) ? __ldg(F + b + 1 + X + XY) : f0, (ox && oy) ? __ldg(F + b + 1 + X) : f0,
-                   (ox && oz) ? __ldg(F + b + 1 + XY) : f0, ox ? __ldg(F + b + 1) : f0,
-                   (oy && oz) ? __ldg(F + b + X + XY) : f0, oy ? __ldg(F + b + X) : f0, oz ? __ldg(F + b + XY) : f0,
-                   __ldg(F + b), cl.a, cl.b, cl.c);
+    return trilerp((ox && oy && oz) ? __ldg(F + b + 1 + Xp + XYp) : f0, (ox && oy) ? __ldg(F + b + 1 + Xp) : f0,
+                   (ox && oz) ? __ldg(F + b + 1 + XYp) : f0, ox ? __ldg(F + b + 1) : f0,
+                   (oy && oz) ? __ldg(F + b + Xp + XYp) : f0, oy ? __ldg(F + b + Xp) : f0,
+                   oz ? __ldg(F + b + XYp) : f0, __ldg(F + b), cl.a, cl.b, cl.c);
 }
 
 __device__ __forceinline__ float4 lerp4_(float4 v0, float4 v1, float t) {

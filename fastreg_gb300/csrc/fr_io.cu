@@ -26,12 +26,12 @@ __global__ void __launch_bounds__(256) pack_init_kernel(IoArgs a) {
         const long long NT = a.NT;
         const int z1 = min(tl.w + kTileZ, P.Z);
         for (int z = tl.w; z < z1; ++z) {
-            const long long i = lin(P, x, y, z);
-            const long long g = P.off + i;
-            a.S[g] = io.img_S[i];
-            a.T[g] = io.img_T[i];
-            a.labS[g] = io.lab_S[i];
-            a.labT[g] = io.lab_T[i];
+            const long long u = user_lin(P, x, y, z);  // caller's layout
+            const long long g = P.off + lin(P, x, y, z);
+            a.S[g] = io.img_S[u];
+            a.T[g] = io.img_T[u];
+            a.labS[g] = io.lab_S[u];
+            a.labT[g] = io.lab_T[u];
             if (a.sobolev) {
                 if (!a.keep_state) {
                     const float pos[3] = {(float)x, (float)y, (float)z};
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) pack_init_kernel(IoArgs a) {
             }
             a.rho0[g] = a.rho_init;
             a.rho1[g] = a.rho_init;
-            a.LT[g] = make_float4(0.f, 0.f, 0.f, io.img_T[i]);  // the Laplacian is 0 on the boundary
+            a.LT[g] = make_float4(0.f, 0.f, 0.f, io.img_T[u]);  // the Laplacian is 0 on the boundary
             if (!a.keep_state) {
                 const float pos[3] = {(float)x, (float)y, (float)z};
 #pragma unroll
@@ -136,10 +136,11 @@ __global__ void __launch_bounds__(256) finalize_kernel(IoArgs a) {
                     wtl = __ldg(labT + ct.base);
                 }
                 if (a.write_outputs) {
-                    io.img_S[i] = ws;
-                    io.lab_S[i] = wl;
-                    io.img_T[i] = wt;
-                    io.lab_T[i] = wtl;
+                    const long long u = user_lin(P, x, y, z);  // caller's layout
+                    io.img_S[u] = ws;
+                    io.lab_S[u] = wl;
+                    io.img_T[u] = wt;
+                    io.lab_T[u] = wtl;
                 }
 
                 // data energy

@@ -30,7 +30,7 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         if (x < 1 || x > P.X - 2 || y < 1 || y > P.Y - 2) continue;
-        const int X = P.X, XY = P.X * P.Y;
+        const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
         const float* __restrict__ Q0 = a.psi + P.off;
         const float* __restrict__ Q1 = Q0 + a.NT;
         const float* __restrict__ Q2 = Q1 + a.NT;
@@ -73,32 +73,32 @@ __device__ __forceinline__ float entropy_flux(float c, float n) {
 // ----------------------------------------------------------------------------------
 // fused pass A
 //
-// A block owns a 32 x 8 column tile and marches z.  The stencil operands (v with a
-// 2-voxel halo and a 5-slice window; psi_inv, rho and S with a 1-voxel halo and a
-// 3-slice window) are staged in shared-memory ring buffers by cp.async one slice
-// ahead of the compute, so the stencil reads are shared-memory loads and the global
-// traffic is one coalesced pass per field.  T o psi_inv and L o psi_inv are gathered
+// A block owns a 32 x 8 column tile and marches z.  The vector stencil operands (v with
+// a 2-voxel halo and a 5-slice window; psi_inv with a 1-voxel halo and a 3-slice window)
+// are staged in shared-memory ring buffers by cp.async kAhead slices ahead of the
+// compute, so their 40 stencil reads per voxel are shared-memory loads and the global
+// traffic is one coalesced pass per field; the scalar stencils (rho, S) go through L1.  T o psi_inv and L o psi_inv are gathered
 // from the interleaved LT field (eight 16-byte loads per voxel).
 // ----------------------------------------------------------------------------------
 namespace {
-constexpr int kVH = 2, kVW = kTileX + 2 * kVH, kVR = kTileY + 2 * kVH, kVS = 7;  // v: halo, width, rows, slots
-constexpr int kQH = 1, kQW = kTileX + 2 * kQH, kQR = kTileY + 2 * kQH, kQS = 5;  // psi_inv, rho, S
+// prefetch distance: slices in flight ahead of the one being computed
+constexpr int kAhead = 2;
+constexpr int kVH = 2, kVW = kTileX + 2 * kVH, kVR = kTileY + 2 * kVH, kVS = 5 + kAhead;  // v: halo, width, rows, slots
+constexpr int kQH = 1, kQW = kTileX + 2 * kQH, kQR = kTileY + 2 * kQH, kQS = 3 + kAhead;  // psi_inv
 constexpr int kVPlane = kVW * kVR, kQPlane = kQW * kQR;
-constexpr int kPassASmemFloats = 3 * kVS * kVPlane + 5 * kQS * kQPlane;  // v x3, psi_inv x3, rho, S
+constexpr int kPassASmemFloats = 3 * kVS * kVPlane + 3 * kQS * kQPlane;  // v x3, psi_inv x3
 constexpr size_t kPassASmemBytes = sizeof(float) * kPassASmemFloats;
 
 struct PassASmem {
     float* v;  // [3][kVS][kVR][kVW]
     float* q;  // [3][kQS][kQR][kQW]
-    float* r;  // [kQS][kQR][kQW]
-    float* s;  // [kQS][kQR][kQW]
 };
 
 // stage one slice zs of a plane with halo h (rows kTileY + 2h, columns 32 + 2h) into
 // dst; cells outside the volume are not loaded (no interior voxel reads them)
 template <int H>
-__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int X, int Y, int Z, int x0,
-                                            int y0, int zs) {
+__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int X, int Y, int Z, int Xp,
+                                            int x0, int y0, int zs) {
     constexpr int W = kTileX + 2 * H, R = kTileY + 2 * H;
     if (zs < 0 || zs >= Z) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -107,7 +107,7 @@ __device__ __forceinline__ void stage_plane(float* dst, const float* __restrict_
     for (int r = warp; r < R; r += kTileY) {
         const int y = y0 - H + r;
         if (y < 0 || y >= Y) continue;
-        const float* row = src + (long long)X * (y + (long long)Y * zs);
+        const float* row = src + (long long)Xp * (y + (long long)Y * zs);
         if (ina) cp_async4(dst + r * W + lane, row + xa);
         if (inb) cp_async4(dst + r * W + 32 + lane, row + xb);
     }
@@ -121,15 +121,14 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
     PassASmem sm;
     sm.v = smem;
     sm.q = sm.v + 3 * kVS * kVPlane;
-    sm.r = sm.q + 3 * kQS * kQPlane;
-    sm.s = sm.r + kQS * kQPlane;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const Tile tl = a.tiles[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
-        const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y, N = (int)P.N;
+        const int X = P.X, Y = P.Y, Z = P.Z, N = (int)P.N;
+        const int Xp = P.Xp, XYp = P.Xp * P.Y;  // strides of the packed arrays
         const int zs0 = max(tl.w, 1), zs1 = min(tl.w + kTileZ, Z - 1);
         if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
         const long long NT = a.NT;
@@ -152,39 +151,40 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
         auto stage_v = [&](int zs) {
             const int sl = vslot(zs);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], X, Y, Z, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], X, Y, Z, Xp, x0, y0, zs);
         };
         auto stage_q = [&](int zs) {
             const int sl = qslot(zs);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], X, Y, Z, x0, y0, zs);
-            stage_plane<kQH>(sm.r + sl * kQPlane, Rg, X, Y, Z, x0, y0, zs);
-            stage_plane<kQH>(sm.s + sl * kQPlane, Sg, X, Y, Z, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], X, Y, Z, Xp, x0, y0, zs);
         };
 
         __syncthreads();  // the previous tile is done with the ring buffers
-        // prologue: everything slice zs0 needs, then what zs0 + 1 adds
+        // prologue: everything slice zs0 needs, then what each of the next kAhead - 1
+        // slices adds (one commit group per slice)
         for (int zs = zs0 - 2; zs <= zs0 + 2; ++zs) stage_v(zs);
         for (int zs = zs0 - 1; zs <= zs0 + 1; ++zs) stage_q(zs);
         cp_async_commit();
-        stage_v(zs0 + 3);
-        stage_q(zs0 + 2);
-        cp_async_commit();
+#pragma unroll
+        for (int k = 1; k < kAhead; ++k) {
+            if (zs0 + 2 + k <= zs1 + 1) stage_v(zs0 + 2 + k);
+            if (zs0 + 1 + k <= zs1) stage_q(zs0 + 1 + k);
+            cp_async_commit();
+        }
 
-        // ring positions of slice z - 2 (v) and z - 1 (psi_inv, rho, S), advanced per slice
+        // ring positions of slice z - 2 (v) and z - 1 (psi_inv), advanced per slice
         int sv = vslot(zs0 - 2), sq = qslot(zs0 - 1);
         const int vc0 = (ty + kVH) * kVW + tx + kVH;
         const int qc0 = (ty + kQH) * kQW + tx + kQH;
         for (int z = zs0; z < zs1; ++z) {
-            cp_async_wait<1>();  // all but the newest group (slice z + 1's) have landed
-            __syncthreads();     // ... for every thread, and slice z - 3 / z - 2 is no longer read
-            // prefetch what slice z + 2 adds; with kVS = 7 and kQS = 5 slots the target
-            // slots are those of slices z - 3 (v) and z - 2 (the others)
-            if (z + 4 <= zs1 + 1) stage_v(z + 4);  // the last slice reads v up to zs1 + 1
-            if (z + 3 <= zs1) stage_q(z + 3);      // and psi_inv, rho, S up to zs1
+            cp_async_wait<kAhead - 1>();  // slice z's group has landed (the newer ones may not)
+            __syncthreads();              // ... for every thread, and slice z - 3 / z - 2 is no longer read
+            // prefetch what slice z + kAhead adds, into the slots of slices z - 3 (v) and z - 2
+            if (z + 2 + kAhead <= zs1 + 1) stage_v(z + 2 + kAhead);  // the last slice reads v up to zs1 + 1
+            if (z + 1 + kAhead <= zs1) stage_q(z + 1 + kAhead);      // and psi_inv up to zs1
             cp_async_commit();
             if (active) {
-                const int i = x + X * y + XY * z;
+                const int i = x + Xp * y + XYp * z;
                 // per-slice base pointers into the rings (immediate offsets below)
                 const float* vb[5][3];
 #pragma unroll
@@ -195,22 +195,18 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                     for (int c = 0; c < 3; ++c) vb[k][c] = sm.v + (c * kVS + sl) * kVPlane + vc0;
                 }
                 const float* qb[3][3];
-                const float* rb[3];
-                const float* sb[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     int sl = sq + k;
                     sl = sl >= kQS ? sl - kQS : sl;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) qb[k][c] = sm.q + (c * kQS + sl) * kQPlane + qc0;
-                    rb[k] = sm.r + sl * kQPlane + qc0;
-                    sb[k] = sm.s + sl * kQPlane + qc0;
                 }
 
                 // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
                 const float q[3] = {qb[1][0][0], qb[1][1][0], qb[1][2][0]};
-                const Cell32 cl = locate32(X, Y, Z, q[0], q[1], q[2]);
-                const float4 lt = tri_unchecked32_f4(LT, X, XY, N, cl);
+                const Cell32 cl = locate32(X, Y, Z, Xp, q[0], q[1], q[2]);
+                const float4 lt = tri_unchecked32_f4(LT, Xp, XYp, N, cl);
                 const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
                 const float Lq[3] = {lt.x, lt.y, lt.z};
 
@@ -225,9 +221,11 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                 const float det = det_ref(M);
 
                 // central-difference gradient of S and the potential gradient
-                const float Si = sb[1][0];
-                const float gs[3] = {(sb[1][1] - sb[1][-1]) * 0.5f, (sb[1][kQW] - sb[1][-kQW]) * 0.5f,
-                                     (sb[2][0] - sb[0][0]) * 0.5f};
+                // rho and S are read through L1 (their 7-point stencils stay in cache)
+                const float Si = __ldg(Sg + i);
+                const float gs[3] = {(__ldg(Sg + i + 1) - __ldg(Sg + i - 1)) * 0.5f,
+                                     (__ldg(Sg + i + Xp) - __ldg(Sg + i - Xp)) * 0.5f,
+                                     (__ldg(Sg + i + XYp) - __ldg(Sg + i - XYp)) * 0.5f};
                 const float diff = Si - Tq;
                 float gU[3];
 #pragma unroll
@@ -248,13 +246,13 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                 const float vx = vc[0], vy = vc[1], vz = vc[2];
 
                 // divergence of rho*v (upwind) and the density update
-                const float p = rb[1][0];
-                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * rb[1][1];
-                const float t12 = (vxm[0] > 0.f) ? vxm[0] * rb[1][-1] : vxm[0] * p;
-                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * rb[1][kQW];
-                const float t22 = (vym[1] > 0.f) ? vym[1] * rb[1][-kQW] : vym[1] * p;
-                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * rb[2][0];
-                const float t32 = (vzm[2] > 0.f) ? vzm[2] * rb[0][0] : vzm[2] * p;
+                const float p = __ldg(Rg + i);
+                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * __ldg(Rg + i + 1);
+                const float t12 = (vxm[0] > 0.f) ? vxm[0] * __ldg(Rg + i - 1) : vxm[0] * p;
+                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * __ldg(Rg + i + Xp);
+                const float t22 = (vym[1] > 0.f) ? vym[1] * __ldg(Rg + i - Xp) : vym[1] * p;
+                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * __ldg(Rg + i + XYp);
+                const float t32 = (vzm[2] > 0.f) ? vzm[2] * __ldg(Rg + i - XYp) : vzm[2] * p;
                 const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
                 const float rho_new = p + a.alpha * div;
                 rho_n[i] = rho_new;
@@ -274,8 +272,8 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 
                 // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
                 // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
-                // reference does; y+2 at y = Y-2 reads linear index i + 2X (voxel
-                // (x, 0, z+1)) from global memory, as the reference's unchecked read does
+                // reference does; y+2 at y = Y-2 reads index i + 2 rows (voxel (x, 0, z+1))
+                // from global memory, as the reference's unchecked read does
                 float dv[3] = {0.f, 0.f, 0.f};
                 if (dv_xy && z >= 2 && z <= Z - 3) {
                     const bool y_edge = y + 2 > Y - 1;
@@ -283,7 +281,7 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                     for (int c = 0; c < 3; ++c) {
                         const float xx = (vx < 0.f) ? (vb[2][c][2] - 2.f * vxp[c]) + vc[c]
                                                     : (vc[c] - 2.f * vxm[c]) + vb[2][c][-2];
-                        const float vyp2 = y_edge ? __ldg(Vg[c] + i + 2 * X) : vb[2][c][2 * kVW];
+                        const float vyp2 = y_edge ? __ldg(Vg[c] + i + 2 * Xp) : vb[2][c][2 * kVW];
                         const float yy = (vy < 0.f) ? (vyp2 - 2.f * vym[c]) + vc[c]
                                                     : (vc[c] - 2.f * vym[c]) + vb[2][c][-2 * kVW];
                         const float zz = (vz < 0.f) ? (vb[4][c][0] - 2.f * vzm[c]) + vc[c]
@@ -331,13 +329,13 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
         unsigned long long best = 0ull;
         if (x >= 1 && x <= P.X - 2 && y >= 1 && y <= P.Y - 2) {
-            const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y;
+            const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XYp = P.Xp * P.Y;
             const long long NT = a.NT;
             // the velocity pass A just wrote
             const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
             float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
             const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
-            int i = x + X * y + XY * z0;
+            int i = x + Xp * y + XYp * z0;
             // psi of the next slice is loaded while this slice's gathers are in flight
             float nx = 0.f, ny = 0.f, nz = 0.f;
             if (z0 < z1) {
@@ -345,17 +343,17 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
                 ny = Q[1][i];
                 nz = Q[2][i];
             }
-            for (int z = z0; z < z1; ++z, i += XY) {
+            for (int z = z0; z < z1; ++z, i += XYp) {
                 const float px = nx, py = ny, pz = nz;
                 if (z + 1 < z1) {
-                    nx = Q[0][i + XY];
-                    ny = Q[1][i + XY];
-                    nz = Q[2][i + XY];
+                    nx = Q[0][i + XYp];
+                    ny = Q[1][i + XYp];
+                    nz = Q[2][i + XYp];
                 }
-                const Cell32 cl = locate32(X, Y, Z, px, py, pz);
-                const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, XY, cl);
-                const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, XY, cl);
-                const float uz = a.alpha * tri_checked32(V[2], X, Y, Z, XY, cl);
+                const Cell32 cl = locate32(X, Y, Z, Xp, px, py, pz);
+                const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, Xp, XYp, cl);
+                const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, Xp, XYp, cl);
+                const float uz = a.alpha * tri_checked32(V[2], X, Y, Z, Xp, XYp, cl);
                 Q[0][i] = px + ux;
                 Q[1][i] = py + uy;
                 Q[2][i] = pz + uz;

@@ -59,7 +59,7 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
         double e = 0.0;
         if (x < P.X && y < P.Y) {
             const long long NT = a.NT;
-            const int X = P.X, XY = P.X * P.Y;
+            const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
             const float* __restrict__ S = a.S + P.off;
             const float* __restrict__ T = a.T + P.off;
             const float* __restrict__ phi0 = a.phi + P.off;
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
         const Tile tl = a.tiles[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
-        const int X = P.X, Y = P.Y, Z = P.Z, XY = P.X * P.Y;
+        const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XY = P.Xp * P.Y;
         const long long NT = a.NT;
         const float* __restrict__ g[3] = {a.g + P.off, a.g + NT + P.off, a.g + 2 * NT + P.off};
         float* m[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
             for (int rr = ty; rr < 3 * H; rr += kSobTileY) {  // one row per warp
                 const int c = rr / H, r = rr - c * H;
                 const int gy = min(max(y0 - R + r, 0), Y - 1);
-                const float* row = g[c] + X * gy + XY * zc;
+                const float* row = g[c] + Xp * gy + XY * zc;
                 cp_async4(&G[buf][c][r][tx], row + xa);
                 if (tx < 2 * R) cp_async4(&G[buf][c][r][32 + tx], row + xb);
             }
@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
             // z pass and momentum for slice zs - R once the ring holds its 2R + 1 slices
             const int x = x0 + tx, y = y0 + ty, zo = zs - R;
             if (k >= 2 * R && x < X && y < Y) {
-                const int i = x + X * y + XY * zo;
+                const int i = x + Xp * y + XY * zo;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     float acc = 0.f;
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
         unsigned long long best = 0ull;
         if (x < P.X && y < P.Y) {
             const long long NT = a.NT;
-            const int X = P.X, XY = P.X * P.Y;
+            const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
             float* phi[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
             const float* __restrict__ mc[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
             const int z1 = min(tl.w + kSobTileZ, P.Z);
