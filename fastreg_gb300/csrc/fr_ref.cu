@@ -83,8 +83,11 @@ __device__ __forceinline__ float entropy_flux(float c, float n) {
 namespace {
 // prefetch distance: slices in flight ahead of the one being computed
 constexpr int kAhead = 2;
-constexpr int kVH = 2, kVW = kTileX + 2 * kVH, kVR = kTileY + 2 * kVH, kVS = 5 + kAhead;  // v: halo, width, rows, slots
-constexpr int kQH = 1, kQW = kTileX + 2 * kQH, kQR = kTileY + 2 * kQH, kQS = 3 + kAhead;  // psi_inv
+// Staged rows cover x0 - 4 .. x0 + 35 (ten aligned 16-byte chunks): column x0 + tx sits
+// at row offset tx + kXO.  v has a 2-row y halo, psi_inv a 1-row one.
+constexpr int kXO = 4, kChunks = (kTileX + 2 * kXO) / 4;
+constexpr int kVH = 2, kVW = kTileX + 2 * kXO, kVR = kTileY + 2 * kVH, kVS = 5 + kAhead;  // v: halo, width, rows, slots
+constexpr int kQH = 1, kQW = kTileX + 2 * kXO, kQR = kTileY + 2 * kQH, kQS = 3 + kAhead;  // psi_inv
 constexpr int kVPlane = kVW * kVR, kQPlane = kQW * kQR;
 constexpr int kPassASmemFloats = 3 * kVS * kVPlane + 3 * kQS * kQPlane;  // v x3, psi_inv x3
 constexpr size_t kPassASmemBytes = sizeof(float) * kPassASmemFloats;
@@ -94,22 +97,19 @@ struct PassASmem {
     float* q;  // [3][kQS][kQR][kQW]
 };
 
-// stage one slice zs of a plane with halo h (rows kTileY + 2h, columns 32 + 2h) into
-// dst; cells outside the volume are not loaded (no interior voxel reads them)
+// stage one slice zs of a plane with y halo H (rows y0 - H .. y0 + 7 + H, columns
+// x0 - 4 .. x0 + 35) into dst with 16-byte copies; chunks and rows outside the padded
+// volume are not loaded (no interior voxel reads them)
 template <int H>
-__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int X, int Y, int Z, int Xp,
-                                            int x0, int y0, int zs) {
-    constexpr int W = kTileX + 2 * H, R = kTileY + 2 * H;
+__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int Y, int Z, int Xp, int x0,
+                                            int y0, int zs) {
+    constexpr int R = kTileY + 2 * H, W = kTileX + 2 * kXO;
     if (zs < 0 || zs >= Z) return;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int xa = x0 - H + lane, xb = x0 - H + 32 + lane;
-    const bool ina = xa >= 0 && xa < X, inb = lane < 2 * H && xb < X;
-    for (int r = warp; r < R; r += kTileY) {
-        const int y = y0 - H + r;
-        if (y < 0 || y >= Y) continue;
-        const float* row = src + (long long)Xp * (y + (long long)Y * zs);
-        if (ina) cp_async4(dst + r * W + lane, row + xa);
-        if (inb) cp_async4(dst + r * W + 32 + lane, row + xb);
+    for (int e = threadIdx.x; e < R * kChunks; e += blockDim.x) {
+        const int r = e / kChunks, k = e - r * kChunks;
+        const int y = y0 - H + r, x = x0 - kXO + 4 * k;
+        if (y < 0 || y >= Y || x < 0 || x >= Xp) continue;
+        cp_async16(dst + r * W + 4 * k, src + (long long)Xp * (y + (long long)Y * zs) + x);
     }
 }
 }  // namespace
@@ -117,7 +117,7 @@ __device__ __forceinline__ void stage_plane(float* dst, const float* __restrict_
 size_t ref_pass_a_smem_bytes() { return kPassASmemBytes; }
 
 __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
-    extern __shared__ float smem[];
+    extern __shared__ __align__(16) float smem[];
     PassASmem sm;
     sm.v = smem;
     sm.q = sm.v + 3 * kVS * kVPlane;
@@ -151,12 +151,12 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
         auto stage_v = [&](int zs) {
             const int sl = vslot(zs);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], X, Y, Z, Xp, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], Y, Z, Xp, x0, y0, zs);
         };
         auto stage_q = [&](int zs) {
             const int sl = qslot(zs);
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], X, Y, Z, Xp, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], Y, Z, Xp, x0, y0, zs);
         };
 
         __syncthreads();  // the previous tile is done with the ring buffers
@@ -174,8 +174,8 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 
         // ring positions of slice z - 2 (v) and z - 1 (psi_inv), advanced per slice
         int sv = vslot(zs0 - 2), sq = qslot(zs0 - 1);
-        const int vc0 = (ty + kVH) * kVW + tx + kVH;
-        const int qc0 = (ty + kQH) * kQW + tx + kQH;
+        const int vc0 = (ty + kVH) * kVW + tx + kXO;
+        const int qc0 = (ty + kQH) * kQW + tx + kXO;
         for (int z = zs0; z < zs1; ++z) {
             cp_async_wait<kAhead - 1>();  // slice z's group has landed (the newer ones may not)
             __syncthreads();              // ... for every thread, and slice z - 3 / z - 2 is no longer read
