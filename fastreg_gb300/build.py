@@ -4,7 +4,9 @@ nvcc compiles every ``csrc/*.cu`` translation unit for sm_103a in parallel and
 links them into ``fastreg_gb300/_lib/libfastreg_gb300.so`` (CUDA runtime linked
 statically, no torch dependency).  ``--fmad=false`` is part of the arithmetic
 contract: the kernels contract no a*b+c on their own; the fused multiply-adds
-they need are written out as fmaf().
+they need are written out as fmaf().  It is given to ptxas as well
+(``-Xptxas --fmad=false``): the front end's flag alone does not stop ptxas from
+fusing a packed f32x2 multiply and add, even ones written with ``.rn``.
 """
 from __future__ import annotations
 
@@ -23,7 +25,7 @@ LIBNAME = "libfastreg_gb300.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
-    "-O3", "-lineinfo", "--fmad=false", "-std=c++17",
+    "-O3", "-lineinfo", "--fmad=false", "-Xptxas", "--fmad=false", "-std=c++17",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
     "--expt-relaxed-constexpr",
 ]

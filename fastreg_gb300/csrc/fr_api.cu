@@ -37,6 +37,9 @@ struct fr_handle {
     long long NT = 0;
     std::vector<Pair> hpairs;
     std::vector<Tile> htiles;
+    // the reference solver's per-kernel tile tables (slices per tile kLapTileZ,
+    // kPassATileZ, kPassBTileZ)
+    std::vector<Tile> htiles_l, htiles_a, htiles_b;
     std::vector<fr_pair> io;  // caller buffers of the current registration
 
     // device memory
@@ -44,6 +47,7 @@ struct fr_handle {
     size_t block_bytes = 0;
     Pair* d_pairs = nullptr;
     Tile* d_tiles = nullptr;
+    Tile *d_tiles_l = nullptr, *d_tiles_a = nullptr, *d_tiles_b = nullptr;
     frg::PairIO* d_io = nullptr;
     float *S = nullptr, *T = nullptr;
     int16_t *labS = nullptr, *labT = nullptr;
@@ -204,6 +208,14 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     h->npairs = n;
     h->hpairs.assign(n, Pair{});
     h->htiles.clear();
+    h->htiles_l.clear();
+    h->htiles_a.clear();
+    h->htiles_b.clear();
+    auto column_tiles = [](std::vector<Tile>& dst, int p, const Pair& P, int depth) {
+        for (int z0 = 0; z0 < P.Z; z0 += depth)
+            for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
+                for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) dst.push_back(make_int4(p, x0, y0, z0));
+    };
     long long off = 0;
     for (int p = 0; p < n; ++p) {
         Pair& P = h->hpairs[p];
@@ -219,6 +231,11 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         for (int z0 = 0; z0 < P.Z; z0 += tz)
             for (int y0 = 0; y0 < P.Y; y0 += ty)
                 for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) h->htiles.push_back(make_int4(p, x0, y0, z0));
+        if (h->P.solver == FR_SOLVER_REFERENCE) {
+            column_tiles(h->htiles_l, p, P, frg::kLapTileZ);
+            column_tiles(h->htiles_a, p, P, frg::kPassATileZ);
+            column_tiles(h->htiles_b, p, P, frg::kPassBTileZ);
+        }
     }
     h->NT = std::max(off, 32LL);
     const long long NT = h->NT;
@@ -234,6 +251,9 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     auto add = [&](void** p, size_t bytes) { slots.push_back({p, bytes}); };
     add((void**)&h->d_pairs, sizeof(Pair) * n);
     add((void**)&h->d_tiles, sizeof(Tile) * ntiles);
+    add((void**)&h->d_tiles_l, sizeof(Tile) * std::max<size_t>(h->htiles_l.size(), 1));
+    add((void**)&h->d_tiles_a, sizeof(Tile) * std::max<size_t>(h->htiles_a.size(), 1));
+    add((void**)&h->d_tiles_b, sizeof(Tile) * std::max<size_t>(h->htiles_b.size(), 1));
     add((void**)&h->d_io, sizeof(frg::PairIO) * n);
     add((void**)&h->S, sizeof(float) * NT);
     add((void**)&h->T, sizeof(float) * NT);
@@ -285,14 +305,19 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     FR_CUDA(h, cudaMemset(h->block, 0, total));
     FR_CUDA(h, cudaMemcpy(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice));
     FR_CUDA(h, cudaMemcpy(h->d_tiles, h->htiles.data(), sizeof(Tile) * ntiles, cudaMemcpyHostToDevice));
+    for (auto tt : {std::make_pair(&h->htiles_l, h->d_tiles_l), std::make_pair(&h->htiles_a, h->d_tiles_a),
+                    std::make_pair(&h->htiles_b, h->d_tiles_b)})
+        if (!tt.first->empty())
+            FR_CUDA(h, cudaMemcpy(tt.second, tt.first->data(), sizeof(Tile) * tt.first->size(), cudaMemcpyHostToDevice));
 
     if (h->P.solver == FR_SOLVER_REFERENCE) {
-        h->grid_lap = occupancy_grid(h, (const void*)frg::ref_laplacian_kernel, ntiles);
+        h->grid_lap = occupancy_grid(h, (const void*)frg::ref_laplacian_kernel, (int)h->htiles_l.size());
         FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)frg::ref_pass_a_smem_bytes()));
-        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, ntiles, frg::ref_pass_a_smem_bytes());
-        h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, ntiles);
+        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, (int)h->htiles_a.size(),
+                                   frg::ref_pass_a_smem_bytes());
+        h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, (int)h->htiles_b.size());
     } else {
         h->grid_a = occupancy_grid(h, (const void*)frg::sob_grad_kernel, ntiles);
         h->grid_lap = occupancy_grid(h, frg::sob_smooth3_fn(h->P.smooth_width / 2), ntiles);
@@ -305,8 +330,12 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
 frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
     frg::RefIterArgs a{};
     a.pairs = h->d_pairs;
-    a.tiles = h->d_tiles;
-    a.ntiles = (int)h->htiles.size();
+    a.tiles_l = h->d_tiles_l;
+    a.ntiles_l = (int)h->htiles_l.size();
+    a.tiles_a = h->d_tiles_a;
+    a.ntiles_a = (int)h->htiles_a.size();
+    a.tiles_b = h->d_tiles_b;
+    a.ntiles_b = (int)h->htiles_b.size();
     a.npairs = h->npairs;
     a.NT = h->NT;
     a.S = h->S;

@@ -32,6 +32,11 @@ typedef int4 Tile;
 constexpr int kTileX = 32;  // threads along x (one warp per row)
 constexpr int kTileY = 8;   // rows per block
 constexpr int kTileZ = 16;  // slices marched by each thread
+// Slices per tile of each reference-mode kernel's own tile table: chosen so that the
+// persistent grids end with a short tail (a tile is the unit of work of one block)
+constexpr int kLapTileZ = 4;     // Laplacian
+constexpr int kPassATileZ = 12;  // pass A (each tile also stages a 4-slice halo)
+constexpr int kPassBTileZ = 8;   // pass B
 
 __device__ __forceinline__ long long lin(const Pair& P, int x, int y, int z) {
     return (long long)x + (long long)P.Xp * ((long long)y + (long long)P.Y * z);

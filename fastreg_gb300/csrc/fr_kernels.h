@@ -12,8 +12,12 @@ namespace frg {
 // Arguments of one reference-mode iteration (all three launches take the same block).
 struct RefIterArgs {
     const Pair* pairs;
-    const Tile* tiles;
-    int ntiles;
+    const Tile* tiles_l;  // 32 x 8 x kLapTileZ tiles (Laplacian)
+    int ntiles_l;
+    const Tile* tiles_a;  // 32 x 8 x kPassATileZ tiles (pass A)
+    int ntiles_a;
+    const Tile* tiles_b;  // 32 x 8 x kPassBTileZ tiles (pass B)
+    int ntiles_b;
     int npairs;
     long long NT;  // packed voxels (plane stride of vector fields)
 

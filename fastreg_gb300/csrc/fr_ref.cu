@@ -24,8 +24,8 @@ namespace frg {
 // (0, 0, 0, T) that pack_init_kernel wrote
 // ----------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_l; t += gridDim.x) {
+        const Tile tl = a.tiles_l[t];
         if (a.stop[tl.x]) continue;
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
         const float* __restrict__ Q2 = Q1 + a.NT;
         const float* __restrict__ T = a.T + P.off;
         float4* LT = a.LT + P.off;
-        const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
+        const int z0 = max(tl.w, 1), z1 = min(tl.w + kLapTileZ, P.Z - 1);
         for (int z = z0; z < z1; ++z) {
             const int i = x + X * y + XY * z;
             float l[3];
@@ -123,13 +123,13 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
     sm.q = sm.v + 3 * kVS * kVPlane;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
 
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_a; t += gridDim.x) {
+        const Tile tl = a.tiles_a[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
         const int X = P.X, Y = P.Y, Z = P.Z, N = (int)P.N;
         const int Xp = P.Xp, XYp = P.Xp * P.Y;  // strides of the packed arrays
-        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + kTileZ, Z - 1);
+        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + kPassATileZ, Z - 1);
         if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
         const long long NT = a.NT;
         const float* __restrict__ Vg[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
@@ -322,8 +322,8 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
     __shared__ unsigned long long red[32];
     __shared__ bool last;
     const int tid = threadIdx.x;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_b; t += gridDim.x) {
+        const Tile tl = a.tiles_b[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
@@ -334,7 +334,7 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
             // the velocity pass A just wrote
             const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
             float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
-            const int z0 = max(tl.w, 1), z1 = min(tl.w + kTileZ, P.Z - 1);
+            const int z0 = max(tl.w, 1), z1 = min(tl.w + kPassBTileZ, P.Z - 1);
             int i = x + Xp * y + XYp * z0;
             // psi of the next slice is loaded while this slice's gathers are in flight
             float nx = 0.f, ny = 0.f, nz = 0.f;
