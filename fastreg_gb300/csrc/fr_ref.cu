@@ -97,20 +97,20 @@ struct PassASmem {
     float* q;  // [3][kQS][kQR][kQW]
 };
 
-// stage one slice zs of a plane with y halo H (rows y0 - H .. y0 + 7 + H, columns
-// x0 - 4 .. x0 + 35) into dst with 16-byte copies; chunks and rows outside the padded
-// volume are not loaded (no interior voxel reads them)
+// A staged slice of a plane with y halo H is R = 8 + 2H rows (y0 - H .. y0 + 7 + H) of
+// kChunks aligned 16-byte chunks (columns x0 - 4 .. x0 + 35).  Thread e copies chunk e of
+// every slice and component of the tile: its shared-memory offset is 4e floats, and its
+// offset inside a slice, fixed for the tile, is returned here (-1: no chunk, or the chunk
+// lies outside the padded volume, where no interior voxel reads).
 template <int H>
-__device__ __forceinline__ void stage_plane(float* dst, const float* __restrict__ src, int Y, int Z, int Xp, int x0,
-                                            int y0, int zs) {
-    constexpr int R = kTileY + 2 * H, W = kTileX + 2 * kXO;
-    if (zs < 0 || zs >= Z) return;
-    for (int e = threadIdx.x; e < R * kChunks; e += blockDim.x) {
-        const int r = e / kChunks, k = e - r * kChunks;
-        const int y = y0 - H + r, x = x0 - kXO + 4 * k;
-        if (y < 0 || y >= Y || x < 0 || x >= Xp) continue;
-        cp_async16(dst + r * W + 4 * k, src + (long long)Xp * (y + (long long)Y * zs) + x);
-    }
+__device__ __forceinline__ int stage_offset(int e, int Y, int Xp, int x0, int y0) {
+    constexpr int R = kTileY + 2 * H;
+    static_assert(R * kChunks <= 256, "one chunk per thread of a 256-thread block");
+    if (e >= R * kChunks) return -1;
+    const int r = e / kChunks, k = e - r * kChunks;
+    const int y = y0 - H + r, x = x0 - kXO + 4 * k;
+    if (y < 0 || y >= Y || x < 0 || x >= Xp) return -1;
+    return Xp * y + x;
 }
 }  // namespace
 
@@ -148,15 +148,21 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 
         auto vslot = [](int zs) { return ((zs % kVS) + kVS) % kVS; };
         auto qslot = [](int zs) { return ((zs % kQS) + kQS) % kQS; };
-        auto stage_v = [&](int zs) {
-            const int sl = vslot(zs);
+        const int gv = stage_offset<kVH>(threadIdx.x, Y, Xp, x0, y0);
+        const int gq = stage_offset<kQH>(threadIdx.x, Y, Xp, x0, y0);
+        auto stage_v = [&](int zs) {  // slice zs of v's three components
+            if (gv < 0 || zs < 0 || zs >= Z) return;
+            float* dst = sm.v + vslot(zs) * kVPlane + 4 * threadIdx.x;
+            const int off = gv + XYp * zs;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kVH>(sm.v + (c * kVS + sl) * kVPlane, Vg[c], Y, Z, Xp, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) cp_async16(dst + c * kVS * kVPlane, Vg[c] + off);
         };
-        auto stage_q = [&](int zs) {
-            const int sl = qslot(zs);
+        auto stage_q = [&](int zs) {  // slice zs of psi_inv's three components
+            if (gq < 0 || zs < 0 || zs >= Z) return;
+            float* dst = sm.q + qslot(zs) * kQPlane + 4 * threadIdx.x;
+            const int off = gq + XYp * zs;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) stage_plane<kQH>(sm.q + (c * kQS + sl) * kQPlane, Qg[c], Y, Z, Xp, x0, y0, zs);
+            for (int c = 0; c < 3; ++c) cp_async16(dst + c * kQS * kQPlane, Qg[c] + off);
         };
 
         __syncthreads();  // the previous tile is done with the ring buffers
