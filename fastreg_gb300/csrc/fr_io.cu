@@ -10,7 +10,8 @@
 //                     pass: SSD energy and regulariser energy in FP64
 //                     (reductor.cpp:45-61), fold count det(I + J_u) <= 0, and the
 //                     per-label Dice counts (solver.cu:9-50) on the GPU
-//   warp_kernel       apply_kernel (vector_fields.cu:81-99) on its own
+//   warp_kernel       apply_kernel (vector_fields.cu:81-99) on its own (warp4_kernel:
+//                     the same, four voxels per thread, for aligned buffers)
 #include "fr_common.cuh"
 #include "fr_kernels.h"
 
@@ -233,6 +234,40 @@ __global__ void __launch_bounds__(256) warp_kernel(const float* __restrict__ pos
         const Cell cl = locate(P, __ldg(pos + i), __ldg(pos + N + i), __ldg(pos + 2 * N + i));
         out[i] = tri_unchecked(img, P, cl);
         if (out_lab) out_lab[i] = __ldg(lab + cl.base);
+    }
+}
+
+// Four consecutive voxels per thread (32-bit indices): 16-byte loads of the three
+// position planes, 32 independent corner loads in flight, a 16-byte store of the
+// intensities and an 8-byte store of the labels.  The caller guarantees N = X*Y*Z a
+// multiple of 4 below 2^31 and 16-byte (pos, out) / 8-byte (out_lab) aligned buffers;
+// per voxel the arithmetic is warp_kernel's.
+__global__ void __launch_bounds__(256) warp4_kernel(const float* __restrict__ pos, const float* __restrict__ img,
+                                                    const int16_t* __restrict__ lab, float* __restrict__ out,
+                                                    int16_t* __restrict__ out_lab, int X, int Y, int Z) {
+    const int N = X * Y * Z, N4 = N >> 2, XY = X * Y;
+    const float4* __restrict__ p4 = reinterpret_cast<const float4*>(pos);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N4; t += gridDim.x * blockDim.x) {
+        const float4 px = __ldg(p4 + t), py = __ldg(p4 + N4 + t), pz = __ldg(p4 + 2 * N4 + t);
+        const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w},
+                    zs[4] = {pz.x, pz.y, pz.z, pz.w};
+        float r[4];
+        int b[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const Cell32 cl = locate32(X, Y, Z, X, xs[k], ys[k], zs[k]);
+            r[k] = tri_unchecked32(img, X, XY, N, cl);
+            b[k] = cl.base;
+        }
+        reinterpret_cast<float4*>(out)[t] = make_float4(r[0], r[1], r[2], r[3]);
+        if (out_lab) {
+            short4 l;
+            l.x = __ldg(lab + b[0]);
+            l.y = __ldg(lab + b[1]);
+            l.z = __ldg(lab + b[2]);
+            l.w = __ldg(lab + b[3]);
+            reinterpret_cast<short4*>(out_lab)[t] = l;
+        }
     }
 }
 
