@@ -198,6 +198,12 @@ __device__ __forceinline__ float4 tri_unchecked32_f4(const float4* __restrict__ 
                   lerp4_(lerp4_(f011, f010, cl.c), lerp4_(f001, f000, cl.c), cl.b), cl.a);
 }
 
+// Hint that the 128-byte line holding *p will be read soon: it is fetched into L2 with
+// no register written and nothing waited for (p must point into an allocation).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // ---- asynchronous global -> shared copies (cp.async, 4 bytes each) ----
 __device__ __forceinline__ void cp_async4(float* smem, const float* gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
