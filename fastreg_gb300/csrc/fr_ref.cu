@@ -367,6 +367,18 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
                     nz = Q[2][i + XYp];
                 }
                 const Cell32 cl = locate32(X, Y, Z, Xp, px, py, pz);
+                {  // L2 prefetch: the v rows the next slice's cell adds (psi is smooth, so that
+                   // cell is about this one plus a slice) and psi two slices on
+                    const int N = (int)P.N, o0 = min(cl.base + 2 * XYp, N - 1), o1 = min(cl.base + 2 * XYp + Xp, N - 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        prefetch_l2(V[c] + o0);
+                        prefetch_l2(V[c] + o1);
+                    }
+                    if (z + 2 < Z)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) prefetch_l2(Q[c] + i + 2 * XYp);
+                }
                 const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, Xp, XYp, cl);
                 const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, Xp, XYp, cl);
                 const float uz = a.alpha * tri_checked32(V[2], X, Y, Z, Xp, XYp, cl);
