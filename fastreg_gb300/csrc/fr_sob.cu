@@ -117,20 +117,27 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
 
 // Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
 // fused with the momentum update m = damping * m - step * gs.  A block owns a 32 x 8
-// column tile: each input slice (tile + R halo, coordinates clamped into the volume)
-// is staged in shared memory by cp.async one slice ahead, smoothed along x and y in
-// shared memory, and pushed into a per-thread register ring of 2R + 1 slices that the
-// z pass reads.  Each tap is one fused multiply-add, acc = fma(w_k, g_k, acc), taken
-// in the order k = -R..R for every axis.
+// column tile and marches z.  Each input slice (the tile's rows plus an R halo, clamped
+// into the volume; columns x0 - HX .. x0 + 31 + HX with HX = R rounded up to 4) is staged
+// in shared memory by 16-byte cp.async NB slices ahead (NB = 3 buffers, 2 for wide
+// kernels, so that the block stays within 48 KB of shared memory).  Per slice step one block
+// barrier separates two independent halves: the x pass of the next slice (shared memory
+// to a double-buffered Gx) and the y pass of this slice (Gx to a per-thread register ring
+// of 2R + 1 slices that the z pass reads).  Columns outside [0, X) are read at the
+// clamped column (only tiles at the x edges take that path).  Each tap is one fused
+// multiply-add, acc = fma(w_k, g_k, acc), taken in the order k = -R..R for every axis.
 template <int R>
 __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
-    constexpr int W = kTileX + 2 * R, H = kSobTileY + 2 * R, K = 2 * R + 1;
-    __shared__ float G[2][3][H][W];
-    __shared__ float Gx[3][H][kTileX];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    float taps[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) taps[k] = a.taps[k];
+    constexpr int HX = (R + 3) / 4 * 4;                // staged x halo: whole 16-byte chunks
+    constexpr int WS = kTileX + 2 * HX, C = WS / 4;    // staged row: floats, chunks
+    constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
+    constexpr int NB = 4 * (3 * 3 * H * WS + 2 * 3 * H * kTileX) <= 48 * 1024 ? 3 : 2;  // staging buffers
+    constexpr int NF = 3 * H * C;                      // chunks of one staged slice
+    constexpr int NJ = (NF + 255) / 256;               // chunks per thread
+    constexpr int RW = (3 * H + kSobTileY - 1) / kSobTileY;  // x-pass rows per warp
+    __shared__ __align__(16) float G[NB][3][H][WS];
+    __shared__ float Gx[2][3][H][kTileX];
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
 
     for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
         const Tile tl = a.tiles[t];
@@ -138,45 +145,86 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
         const Pair P = a.pairs[tl.x];
         const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XY = P.Xp * P.Y;
         const long long NT = a.NT;
-        const float* __restrict__ g[3] = {a.g + P.off, a.g + NT + P.off, a.g + 2 * NT + P.off};
+        const float* __restrict__ g0 = a.g + P.off;
         float* m[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
         const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + kSobTileZ, Z);
         const int nsl = (zt1 - zt0) + 2 * R;
+        const bool xedge = x0 - R < 0 || x0 + kTileX - 1 + R > X - 1;  // uniform over the block
 
-        // clamped x of this lane's staged columns (replicate boundary)
-        const int xa = min(max(x0 - R + tx, 0), X - 1);
-        const int xb = min(max(x0 - R + 32 + tx, 0), X - 1);
-        auto stage = [&](int zs, int buf) {
-            const int zc = min(max(zs, 0), Z - 1);
-            for (int rr = ty; rr < 3 * H; rr += kSobTileY) {  // one row per warp
-                const int c = rr / H, r = rr - c * H;
-                const int gy = min(max(y0 - R + r, 0), Y - 1);
-                const float* row = g[c] + Xp * gy + XY * zc;
-                cp_async4(&G[buf][c][r][tx], row + xa);
-                if (tx < 2 * R) cp_async4(&G[buf][c][r][32 + tx], row + xb);
+        // chunk f = tid + 256 j of a staged slice is (component c, row r, chunk k); its
+        // shared-memory offset is 4 f floats and its offset inside a slice of component c
+        // is fixed for the tile (-1: the chunk lies outside the padded row, never read)
+        int goff[NJ];
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            const int f = tid + 256 * j;
+            goff[j] = -1;
+            if (f < NF) {
+                const int c = f / (H * C), rem = f - c * (H * C), r = rem / C, k = rem - r * C;
+                const int gy = min(max(y0 - R + r, 0), Y - 1), xs = x0 - HX + 4 * k;
+                if (xs >= 0 && xs < Xp) goff[j] = Xp * gy + xs;
+            }
+        }
+        auto stage = [&](int k) {  // staged slice k of the tile (z = zt0 - R + k, clamped)
+            if (k >= nsl) return;
+            const long long zoff = (long long)XY * min(max(zt0 - R + k, 0), Z - 1);
+            float* dst = &G[k % NB][0][0][0];
+#pragma unroll
+            for (int j = 0; j < NJ; ++j) {
+                const int f = tid + 256 * j;
+                if (goff[j] >= 0) cp_async16(dst + 4 * f, g0 + (f / (H * C)) * NT + zoff + goff[j]);
+            }
+        };
+        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
+            const float* src = &G[k % NB][0][0][0];
+            float* dst = &Gx[k & 1][0][0][0];
+#pragma unroll
+            for (int j = 0; j < RW; ++j) {
+                const int rr = ty + kSobTileY * j;  // row rr of the 3 H staged rows
+                if (rr < 3 * H) {
+                    const float* row = src + rr * WS;
+                    float acc = 0.f;
+                    if (!xedge) {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], row[HX - R + tx + q], acc);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) {
+                            const int xi = min(max(x0 - R + tx + q, 0), X - 1);
+                            acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
+                        }
+                    }
+                    dst[rr * kTileX + tx] = acc;
+                }
             }
         };
 
+        // this thread's column; its momentum is loaded one output slice ahead
+        const int x = x0 + tx, y = y0 + ty, col = x + Xp * y;
+        const bool inside = x < X && y < Y;
+        float mv[3] = {0.f, 0.f, 0.f};
+        if (inside)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) mv[c] = m[c][col + XY * zt0];
+
         float ring[K][3];
         __syncthreads();  // the previous tile is done with G and Gx
-        stage(zt0 - R, 0);
-        cp_async_commit();
-        for (int k = 0; k < nsl; ++k) {
-            const int zs = zt0 - R + k, buf = k & 1;
-            if (k + 1 < nsl) stage(zs + 1, buf ^ 1);
-            cp_async_commit();
-            cp_async_wait<1>();
-            __syncthreads();
-            // x pass over the tile rows and the y halo, one row per warp
-            for (int rr = ty; rr < 3 * H; rr += kSobTileY) {
-                const int c = rr / H, r = rr - c * H;
-                float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], G[buf][c][r][tx + q], acc);
-                Gx[c][r][tx] = acc;
-            }
-            __syncthreads();
-            // y pass for this thread's column, pushed into the z ring
+        for (int k = 0; k < NB; ++k) {
+            stage(k);
+            cp_async_commit();
+        }
+        cp_async_wait<NB - 1>();  // slice 0 has landed
+        __syncthreads();
+        x_pass(0);
+        for (int k = 0; k < nsl; ++k) {
+            cp_async_wait<NB - 2>();  // slice k + 1 has landed (the later ones may not)
+            __syncthreads();          // ... for every thread; Gx[k & 1] is complete; slice k's buffer
+                                      // and Gx[(k + 1) & 1] are no longer read
+            stage(k + NB);            // into slice k's buffer
+            cp_async_commit();
+            if (k + 1 < nsl) x_pass(k + 1);
+            // y pass of slice k for this thread's column, pushed into the z ring
 #pragma unroll
             for (int q = 0; q < K - 1; ++q)
 #pragma unroll
@@ -185,19 +233,21 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
             for (int c = 0; c < 3; ++c) {
                 float acc = 0.f;
 #pragma unroll
-                for (int q = 0; q < K; ++q) acc = fmaf(taps[q], Gx[c][ty + q][tx], acc);
+                for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], Gx[k & 1][c][ty + q][tx], acc);
                 ring[K - 1][c] = acc;
             }
-            // z pass and momentum for slice zs - R once the ring holds its 2R + 1 slices
-            const int x = x0 + tx, y = y0 + ty, zo = zs - R;
-            if (k >= 2 * R && x < X && y < Y) {
-                const int i = x + Xp * y + XY * zo;
+            // z pass and momentum for slice zt0 + k - 2R once the ring holds its 2R + 1 slices
+            const int zo = zt0 - 2 * R + k;
+            if (k >= 2 * R && inside) {
+                const int i = col + XY * zo;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
                     float acc = 0.f;
 #pragma unroll
-                    for (int q = 0; q < K; ++q) acc = fmaf(taps[q], ring[q][c], acc);
-                    m[c][i] = a.damping * m[c][i] - a.step * acc;
+                    for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], ring[q][c], acc);
+                    const float mo = mv[c];
+                    if (zo + 1 < zt1) mv[c] = m[c][i + XY];  // the next output slice's momentum
+                    m[c][i] = a.damping * mo - a.step * acc;
                 }
             }
         }

@@ -70,3 +70,20 @@ def test_sobolev_registration(cuda, dims):
     o64 = O.sob_register(P, d["T"], d["S"], prec=64)
     err = np.abs(phi - o64["phi"]).max()
     assert err < 1e-3, f"phi vs FP64 oracle: max abs err {err} voxels"
+
+
+@pytest.mark.parametrize("width", [1, 3, 9, 11, 15])
+def test_sobolev_smoothing_widths(cuda, width):
+    """Every smoothing radius (one kernel instance per radius: 16-byte staging with an x
+    halo of 4 or 8 columns, 3 or 2 staging buffers, clamped columns on edge tiles) gives
+    the oracle's bits; odd sizes put most tiles on an x edge."""
+    dims = (37, 19, 23)
+    d = images(dims, 300 + width)
+    P = Params(volume_dims=dims, no_labels=4, max_iter=6, solver="sobolev", smooth_sigma=0.4 + 0.3 * width,
+               smooth_width=width, damping=0.9, step=0.5)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    o = O.sob_register(P, d["T"], d["S"])
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["phi"], f"phi (width {width})")
+    assert_bitexact(fr.get_field(N.FR_FIELD_V).cpu().numpy(), o["m"], f"momentum (width {width})")
