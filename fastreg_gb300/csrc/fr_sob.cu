@@ -281,6 +281,19 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
                     nz = phi[2][i + XY];
                 }
                 const SobCell s = sob_locate(P, px, py, pz);
+                {  // L2 prefetch: the m rows the next slice's cell adds (phi is smooth, so that
+                   // cell is about this one plus a slice) and phi two slices on
+                    const int N = (int)P.N, o0 = min((int)s.base + 2 * XY, N - 1);
+                    const int o1 = min((int)s.base + 2 * XY + X, N - 1);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        prefetch_l2(mc[c] + o0);
+                        prefetch_l2(mc[c] + o1);
+                    }
+                    if (z + 2 < P.Z)
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) prefetch_l2(phi[c] + i + 2 * XY);
+                }
                 float u[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
