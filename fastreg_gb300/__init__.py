@@ -4,7 +4,7 @@ The product is the C ABI in include/fastreg_gb300.h, implemented by the
 in-tree library fastreg_gb300/_lib/libfastreg_gb300.so; this package is its
 Python mirror of the reference's Params / FastReg interface.
 """
-from .fastreg import FastReg, Params, Stats, warp  # noqa: F401
+from .fastreg import FastReg, Params, Stats, estimate_inverse, interpolate_field, warp  # noqa: F401
 from . import _native  # noqa: F401
 
-__all__ = ["FastReg", "Params", "Stats", "warp"]
+__all__ = ["FastReg", "Params", "Stats", "estimate_inverse", "interpolate_field", "warp"]

@@ -104,6 +104,8 @@ SIGNATURES = [
     ("fr_finish", C.c_int, [C.c_void_p, C.c_void_p]),
     ("fr_time_kernels", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     ("fr_warp", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fr_estimate_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p]),
+    ("fr_interpolate_field", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]),
     ("fr_sobolev_loss_grad", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_float, C.c_int,
                                        C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, C.POINTER(C.c_double),
                                        C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),

@@ -1105,4 +1105,76 @@ int fr_warp(const float* d_pos, const float* d_img, const int16_t* d_lab, const 
     return FR_OK;
 }
 
+static int field_op_check(const void* a, const void* b, const void* c, const int dims[3], const char* who) {
+    g_parse_error.clear();
+    if (!a || !b || !c || !dims) {
+        g_parse_error = std::string(who) + ": NULL argument";
+        return FR_ERR_INVALID_ARG;
+    }
+    if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || (long long)dims[0] * dims[1] * dims[2] > 0x7fffffffLL) {
+        g_parse_error = std::string(who) + ": dims must be >= 1 with at most 2^31-1 voxels";
+        return FR_ERR_INVALID_ARG;
+    }
+    return FR_OK;
+}
+
+static int field_op_launch(const void* fn, long long work, const char* who, void (*launch)(int grid, void* ctx),
+                           void* ctx) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
+    const int grid =
+        (int)std::max(1LL, std::min<long long>((work + 255) / 256, (long long)std::max(per_sm, 1) * std::max(sms, 1)));
+    launch(grid, ctx);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        g_parse_error = std::string(who) + ": " + cudaGetErrorString(e);
+        return FR_ERR_CUDA;
+    }
+    return FR_OK;
+}
+
+int fr_estimate_inverse(const float* d_psi, float* d_psi_inv, const int dims[3], int sweeps, void* stream) {
+    int rc = field_op_check(d_psi, d_psi_inv, d_psi_inv, dims, "fr_estimate_inverse");
+    if (rc != FR_OK) return rc;
+    if (sweeps < 0) {
+        g_parse_error = "fr_estimate_inverse: sweeps must be >= 0";
+        return FR_ERR_INVALID_ARG;
+    }
+    struct Ctx {
+        const float* psi;
+        float* pinv;
+        const int* d;
+        int sweeps;
+        cudaStream_t s;
+    } c{d_psi, d_psi_inv, dims, sweeps, (cudaStream_t)stream};
+    return field_op_launch(
+        (const void*)frg::estimate_inverse_kernel, (long long)dims[0] * dims[1] * dims[2], "fr_estimate_inverse",
+        [](int grid, void* p) {
+            Ctx* c = (Ctx*)p;
+            frg::estimate_inverse_kernel<<<grid, 256, 0, c->s>>>(c->psi, c->pinv, c->d[0], c->d[1], c->d[2], c->sweeps);
+        },
+        &c);
+}
+
+int fr_interpolate_field(const float* d_field, const float* d_pos, const int dims[3], float* d_out, void* stream) {
+    int rc = field_op_check(d_field, d_pos, d_out, dims, "fr_interpolate_field");
+    if (rc != FR_OK) return rc;
+    struct Ctx {
+        const float* f;
+        const float* pos;
+        float* out;
+        const int* d;
+        cudaStream_t s;
+    } c{d_field, d_pos, d_out, dims, (cudaStream_t)stream};
+    return field_op_launch(
+        (const void*)frg::interpolate_field_kernel, (long long)dims[0] * dims[1] * dims[2], "fr_interpolate_field",
+        [](int grid, void* p) {
+            Ctx* c = (Ctx*)p;
+            frg::interpolate_field_kernel<<<grid, 256, 0, c->s>>>(c->f, c->pos, c->out, c->d[0], c->d[1], c->d[2]);
+        },
+        &c);
+}
+
 }  // extern "C"

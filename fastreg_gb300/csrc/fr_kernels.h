@@ -104,5 +104,8 @@ __global__ void warp_kernel(const float* __restrict__ pos, const float* __restri
                             int16_t* __restrict__ out_lab, Pair P);
 __global__ void warp4_kernel(const float* pos, const float* img, const int16_t* lab, float* out, int16_t* out_lab, int X,
                              int Y, int Z);
+// the reference's unused field kernels (fr_fields.cu)
+__global__ void estimate_inverse_kernel(const float* psi, float* psi_inv, int X, int Y, int Z, int sweeps);
+__global__ void interpolate_field_kernel(const float* field, const float* pos, float* out, int X, int Y, int Z);
 
 }  // namespace frg

@@ -277,3 +277,33 @@ def warp(pos, img, lab=None, stream=None, out=None, out_lab=None):
     N.check(lib.fr_warp(_ptr(pos), _ptr(img), _ptr(lab) if lab is not None else None, dims, _ptr(out),
                         _ptr(out_lab) if out_lab is not None else None, _stream_ptr(stream)), None, "fr_warp")
     return (out, out_lab) if lab is not None else out
+
+
+def estimate_inverse(psi, psi_inv, sweeps=48, stream=None):
+    """DeformationField::get_inverse (vector_fields.cpp:96-103, vector_fields.cu:109-136):
+    `sweeps` passes of psi_inv <- -(psi o psi_inv), psi_inv (3, Z, Y, X) updated in place
+    and returned."""
+    lib = N.load()
+    if tuple(psi.shape) != tuple(psi_inv.shape) or psi.dim() != 4 or psi.shape[0] != 3:
+        raise ValueError("psi and psi_inv must both be (3, Z, Y, X)")
+    _, z, y, x = psi.shape
+    dims = (C.c_int * 3)(x, y, z)
+    N.check(lib.fr_estimate_inverse(_ptr(psi), _ptr(psi_inv), dims, int(sweeps), _stream_ptr(stream)), None,
+            "fr_estimate_inverse")
+    return psi_inv
+
+
+def interpolate_field(field, pos, out=None, stream=None):
+    """interpolate_gradient (vector_fields.cu:194-225): a (3, Z, Y, X) field sampled at
+    the positions pos (3, Z, Y, X)."""
+    import torch
+    lib = N.load()
+    if tuple(field.shape) != tuple(pos.shape) or field.dim() != 4 or field.shape[0] != 3:
+        raise ValueError("field and pos must both be (3, Z, Y, X)")
+    if out is None:
+        out = torch.empty_like(field)
+    _, z, y, x = field.shape
+    dims = (C.c_int * 3)(x, y, z)
+    N.check(lib.fr_interpolate_field(_ptr(field), _ptr(pos), dims, _ptr(out), _stream_ptr(stream)), None,
+            "fr_interpolate_field")
+    return out

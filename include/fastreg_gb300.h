@@ -146,6 +146,18 @@ int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *st
 int fr_warp(const float *d_pos, const float *d_img, const int16_t *d_lab, const int dims[3], float *d_out,
             int16_t *d_out_lab, void *stream);
 
+/* The reference's DeformationField::get_inverse / estimate_inverse
+ * (src/fastreg/vector_fields.cpp:96-103, src/fastreg/cuda/vector_fields.cu:109-136),
+ * which its registration never calls: `sweeps` passes (48 in the reference) of
+ *   psi_inv(x) <- -(psi o psi_inv(x))     (unchecked trilinear sample, every voxel)
+ * with d_psi_inv (3 planes of N floats, device) updated in place.  Same results as the
+ * reference's 48 launches, in one launch. */
+int fr_estimate_inverse(const float *d_psi, float *d_psi_inv, const int dims[3], int sweeps, void *stream);
+
+/* The reference's interpolate_gradient (src/fastreg/cuda/vector_fields.cu:194-225): a
+ * 3-component field (3 planes of N) sampled at the positions d_pos (3 planes) into d_out. */
+int fr_interpolate_field(const float *d_field, const float *d_pos, const int dims[3], float *d_out, void *stream);
+
 /* ---- the differentiated sobolev registration (no counterpart in the reference) ----
  * J(v0, lambda) = 0.5 * sum (S(phi_K) - T)^2 + 0.1 * sum |m_K|^2 after `iters` sobolev
  * iterations (damping, step, smooth_sigma, smooth_width as the SOLVER=sobolev keys) from

@@ -159,6 +159,44 @@ void FN(warp)(const int *dims, const real *pos, const real *img, const int16_t *
     }
 }
 
+/* estimate_inverse (src/fastreg/cuda/vector_fields.cu:109-136; the reference's
+ * registration never calls it): `sweeps` passes (48 in the reference) of
+ *   psi_inv(x) <- -interpolate_field(psi, trunc(psi_inv(x)))
+ * over every voxel, in place.  interpolate_field is the unchecked vector trilinear
+ * sample (include/cuda/cuda_utils.hpp:86-107) and trunc keeps x, y, z
+ * (cuda_utils.hpp:264).  A voxel's update reads only its own previous value (the
+ * gather is from psi), so its sweeps can run back to back. */
+void FN(estimate_inverse)(const int *dims, const real *psi, real *psi_inv, int sweeps) {
+    fro_dims d = {dims[0], dims[1], dims[2]};
+    const int64_t N = nvox(&d);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) {
+        real p[3] = {psi_inv[i], psi_inv[N + i], psi_inv[2 * N + i]};
+        for (int s = 0; s < sweeps; ++s) {
+            fro_cell cl;
+            locate_(&d, p[0], p[1], p[2], &cl);
+            real q[3];
+            for (int c = 0; c < 3; ++c) q[c] = R(-1) * tri_unchecked_(psi + c * N, &d, &cl);
+            for (int c = 0; c < 3; ++c) p[c] = q[c];
+        }
+        for (int c = 0; c < 3; ++c) psi_inv[c * N + i] = p[c];
+    }
+}
+
+/* interpolate_gradient (src/fastreg/cuda/vector_fields.cu:194-225; not called by the
+ * reference's registration): out(x) = interpolate_field(field, trunc(pos(x))) over
+ * every voxel, for any 3-component field. */
+void FN(interpolate_field)(const int *dims, const real *field, const real *pos, real *out) {
+    fro_dims d = {dims[0], dims[1], dims[2]};
+    const int64_t N = nvox(&d);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) {
+        fro_cell cl;
+        locate_(&d, pos[i], pos[N + i], pos[2 * N + i], &cl);
+        for (int c = 0; c < 3; ++c) out[c * N + i] = tri_unchecked_(field + c * N, &d, &cl);
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* Reference mode: one iteration of estimate_psi (solver.cu:329-433)          */
 /* ------------------------------------------------------------------------- */

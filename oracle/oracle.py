@@ -131,6 +131,23 @@ def warp(pos, img, lab=None, prec=32):
     return (out, out_lab) if lab is not None else out
 
 
+def estimate_inverse(psi, psi_inv, sweeps=48, prec=32):
+    """The reference's estimate_inverse: `sweeps` in-place passes of
+    psi_inv <- -psi o psi_inv (3-plane fields); returns the final psi_inv."""
+    psi = _f(psi, prec)
+    out = _f(psi_inv, prec).copy()
+    getattr(lib(prec), f"fro{prec}_estimate_inverse")(_dims(psi.shape[1:]), _p(psi), _p(out), int(sweeps))
+    return out
+
+
+def interpolate_field(field, pos, prec=32):
+    """The reference's interpolate_gradient: a 3-plane field sampled at pos."""
+    field, pos = _f(field, prec), _f(pos, prec)
+    out = np.empty_like(field)
+    getattr(lib(prec), f"fro{prec}_interpolate_field")(_dims(field.shape[1:]), _p(field), _p(pos), _p(out))
+    return out
+
+
 def warp_nearest_label(pos, lab, prec=32):
     pos = _f(pos, prec)
     lab = np.ascontiguousarray(lab, dtype=np.int16)

@@ -359,3 +359,81 @@ done:
     if (ctx) cuDevicePrimaryCtxRelease(dev);
     return ran;
 }
+
+/* The reference's two field kernels that its registration never calls
+ * (src/fastreg/cuda/vector_fields.cu:109-136,194-225), run as its host code would:
+ *   op 0  estimate_inverse (vector_fields.cu:125-136): `sweeps` launches (48 in the
+ *         reference) of estimate_inverse_kernel(psi, psi_inv), psi_inv updated in place;
+ *         a is psi, b the initial psi_inv, out the final psi_inv;
+ *   op 1  interpolate_gradient (vector_fields.cu:217-225): interpolate_gradient_kernel(
+ *         field, out, psi); a is psi, b the field, out = field o psi.
+ * Host arrays are 3 planes of N floats (packed to and from float4 with w = 0); every
+ * buffer has the zeroed tail described in rr_register.  Returns 0, or -1. */
+int rr_field_op(const char *cubin_dir, const int *dims, int op, int sweeps, const float *a, const float *b,
+                float *out) {
+    CUmodule mod = 0;
+    CUdeviceptr bufs[3] = {0, 0, 0};
+    CUstream st = 0;
+    CUcontext ctx = 0;
+    CUdevice dev = 0;
+    int rc = -1;
+    const int X = dims[0], Y = dims[1], Z = dims[2];
+    const size_t N = (size_t)X * Y * Z;
+    const size_t tail = ((size_t)X * Y + X + 64) * 16;
+    float *h = (float *)calloc(N * 4, sizeof(float));
+    if (!h) {
+        snprintf(g_err, sizeof g_err, "out of host memory");
+        return -1;
+    }
+    CK(cuInit(0));
+    CK(cuDeviceGet(&dev, 0));
+    CK(cuDevicePrimaryCtxRetain(&ctx, dev));
+    CK(cuCtxSetCurrent(ctx));
+    {
+        char path[1024];
+        snprintf(path, sizeof path, "%s/%s", cubin_dir, MOD_FILES[M_VF]);
+        CK(cuModuleLoad(&mod, path));
+    }
+    CK(cuStreamCreate(&st, CU_STREAM_NON_BLOCKING));
+    CUfunction k;
+    if (find_fn(mod, op == 0 ? "estimate_inverse_kernel" : "interpolate_gradient_kernel", 'E', NULL, &k)) goto fail;
+    for (int j = 0; j < 3; ++j) {
+        CK(cuMemAlloc(&bufs[j], N * 16 + tail));
+        CK(cuMemsetD8(bufs[j], 0, N * 16 + tail));
+    }
+    const float *src[2] = {a, b};
+    for (int j = 0; j < 2; ++j) {
+        for (size_t i = 0; i < N; ++i)
+            for (int c = 0; c < 3; ++c) h[4 * i + c] = src[j][c * N + i];
+        CK(cuMemcpyHtoD(bufs[j], h, N * 16));
+    }
+    rr_view va = {bufs[0], {X, Y, Z}, 0}, vb = {bufs[1], {X, Y, Z}, 0}, vo = {bufs[2], {X, Y, Z}, 0};
+    CUdeviceptr result = bufs[2];
+    if (op == 0) {
+        void *args[] = {&va, &vb};
+        for (int s = 0; s < sweeps; ++s) {
+            CK(launch2d(k, X, Y, 64, 16, st, args));
+            CK(cuStreamSynchronize(st));
+        }
+        result = bufs[1];
+    } else {
+        void *args[] = {&vb, &vo, &va};
+        CK(launch2d(k, X, Y, 64, 16, st, args));
+    }
+    CK(cuStreamSynchronize(st));
+    CK(cuMemcpyDtoH(h, result, N * 16));
+    for (size_t i = 0; i < N; ++i)
+        for (int c = 0; c < 3; ++c) out[c * N + i] = h[4 * i + c];
+    rc = 0;
+    goto done;
+fail:
+    rc = -1;
+done:
+    free(h);
+    for (int j = 0; j < 3; ++j)
+        if (bufs[j]) cuMemFree(bufs[j]);
+    if (st) cuStreamDestroy(st);
+    if (mod) cuModuleUnload(mod);
+    if (ctx) cuDevicePrimaryCtxRelease(dev);
+    return rc;
+}

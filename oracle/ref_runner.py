@@ -30,8 +30,33 @@ def _lib():
         ref_build.build_runner()
     lib = C.CDLL(str(path))
     lib.rr_register.restype = C.c_int
+    lib.rr_field_op.restype = C.c_int
     lib.rr_last_error.restype = C.c_char_p
     return lib
+
+
+def _field_op(op, a, b, sweeps=0):
+    lib = _lib()
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    _, z, y, x = a.shape
+    out = np.empty_like(a)
+    dims = (C.c_int * 3)(x, y, z)
+    p = lambda v: v.ctypes.data_as(C.c_void_p)  # noqa: E731
+    if lib.rr_field_op(str(REF_DIR).encode(), dims, op, int(sweeps), p(a), p(b), p(out)) != 0:
+        raise RuntimeError("reference run failed: " + lib.rr_last_error().decode())
+    return out
+
+
+def estimate_inverse(psi, psi_inv, sweeps=48):
+    """The reference's DeformationField::get_inverse (vector_fields.cpp:96-103): `sweeps`
+    launches of estimate_inverse_kernel, psi_inv (3 planes) updated in place; returns it."""
+    return _field_op(0, psi, psi_inv, sweeps)
+
+
+def interpolate_gradient(field, psi):
+    """The reference's interpolate_gradient: field (3 planes) sampled at psi."""
+    return _field_op(1, psi, field)
 
 
 def register(params, T, labT, S, labS, timing=False):

@@ -6,6 +6,9 @@ oracle/ref_runner.c -- on seeded synthetic pairs, and stores inputs, parameters 
 outputs as compressed .npz files.  Needs a GPU; run from the repository root:
 
     python tests/golden/make_golden.py [out_dir]      (default: tests/golden)
+
+It also runs the reference's two field kernels that its registration never calls
+(estimate_inverse, interpolate_gradient) on seeded fields (field_ops.npz).
 """
 from __future__ import annotations
 
@@ -42,12 +45,34 @@ def case_inputs(dims, seed):
     return sy.make_pair(spec)
 
 
+def field_inputs(dims, seed):
+    """psi for estimate_inverse: -(c + 0.3 (x - c) + noise), c the centre of the grid, so
+    that -psi o p stays inside the grid and the 48 sweeps do not collapse onto a corner;
+    the initial psi_inv is the identity.  For interpolate_gradient: a N(0, 1) field and
+    positions identity + N(0, 1.5) noise, some outside the grid, plus a NaN."""
+    r = np.random.Generator(np.random.PCG64(seed))
+    X, Y, Z = dims
+    z, y, x = np.meshgrid(np.arange(Z), np.arange(Y), np.arange(X), indexing="ij")
+    idn = np.stack([x, y, z]).astype(np.float64)
+    c = np.array([(X - 1) / 2, (Y - 1) / 2, (Z - 1) / 2]).reshape(3, 1, 1, 1)
+    psi = -(c + 0.3 * (idn - c) + r.normal(0, 0.5, idn.shape))
+    field = r.normal(0, 1, idn.shape)
+    pos = idn + r.normal(0, 1.5, idn.shape)
+    pos[:, 0, 0, 0] = np.nan
+    f32 = lambda a: a.astype(np.float32)  # noqa: E731
+    return f32(psi), f32(idn), f32(field), f32(pos)
+
+
+FIELD_CASES = {"13x11x9": ((13, 11, 9), 201), "30x22x17": ((30, 22, 17), 202)}
+
+
 def main(out_dir: Path):
     if not ref_runner.available():
         raise SystemExit("reference cubins missing: build them with oracle/ref_build.py where the reference "
                          "sources are present")
     out_dir.mkdir(parents=True, exist_ok=True)
-    for name, (dims, seed, kw) in CASES.items():
+    only_fields = "--fields-only" in sys.argv
+    for name, (dims, seed, kw) in ({} if only_fields else CASES).items():
         P = case_params(dims, kw)
         d = case_inputs(dims, seed)
         r = ref_runner.register(P, d["T"], d["labT"], d["S"], d["labS"])
@@ -57,7 +82,17 @@ def main(out_dir: Path):
                             S=d["S"], labS=d["labS"], **{k: v for k, v in r.items() if k != "iterations"},
                             iterations=np.array(r["iterations"]))
         print(f"{name}: {r['iterations']} iterations, last max update norm {r['trace_norm'][-1]:.6g}")
+    arrays = {}
+    for name, (dims, seed) in FIELD_CASES.items():
+        psi, psi_inv0, field, pos = field_inputs(dims, seed)
+        arrays[f"{name}_psi"], arrays[f"{name}_psi_inv0"] = psi, psi_inv0
+        arrays[f"{name}_field"], arrays[f"{name}_pos"] = field, pos
+        arrays[f"{name}_psi_inv48"] = ref_runner.estimate_inverse(psi, psi_inv0, 48)
+        arrays[f"{name}_field_o_pos"] = ref_runner.interpolate_gradient(field, pos)
+        print(f"field ops {name}: done")
+    np.savez_compressed(out_dir / "field_ops.npz", **arrays)
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else ROOT / "tests" / "golden")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    main(Path(args[0]) if args else ROOT / "tests" / "golden")

@@ -65,3 +65,28 @@ def test_oracle_matches_reference_kernels(path):
         assert np.array_equal(o[k], f[k]), f"{k} not identical"
     assert err.max() <= 1e-6
     assert np.array_equal(o["trace_idx"], f["trace_idx"])
+
+
+FIELD_OPS = Path(__file__).resolve().parent.joinpath("golden", "field_ops.npz")
+
+
+def _field_cases():
+    f = np.load(FIELD_OPS)
+    return f, sorted({k.split("_")[0] for k in f.files})
+
+
+def test_field_ops_oracle_matches_reference_kernels():
+    """estimate_inverse (48 sweeps) and interpolate_gradient, the reference's two field
+    kernels its registration never calls: the oracle against the reference build's
+    outputs, bit for bit (the sweeps are FMA-free lerps of stored values, so the build's
+    contraction and approximate division do not enter)."""
+    assert FIELD_OPS.exists(), "tests/golden/field_ops.npz is missing: run tests/golden/make_golden.py"
+    f, names = _field_cases()
+    assert names
+    for n in names:
+        inv = O.estimate_inverse(f[f"{n}_psi"], f[f"{n}_psi_inv0"], 48)
+        np.testing.assert_array_equal(inv.view(np.uint32), f[f"{n}_psi_inv48"].view(np.uint32), err_msg=n)
+        out = O.interpolate_field(f[f"{n}_field"], f[f"{n}_pos"])
+        ref = f[f"{n}_field_o_pos"]
+        same = (out.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(out) & np.isnan(ref))
+        assert same.all(), f"{n}: {int((~same).sum())} samples differ"

@@ -223,3 +223,34 @@ def test_verbose_mode_prints_and_matches_graph_mode(cuda, capfd):
     assert_bitexact(out[1][0], out[0][0], "psi (verbose vs graph)")
     assert_bitexact(out[1][1], out[0][1], "S o psi (verbose vs graph)")
     assert out[1][2].e_data == out[0][2].e_data
+
+
+def test_field_ops_vs_oracle_and_reference(cuda):
+    """fr_estimate_inverse (one launch, all sweeps per thread) and fr_interpolate_field
+    against the oracle bit for bit, on the golden inputs and on odd-sized random fields,
+    and against the reference's own kernels run here when their cubins are present."""
+    import torch
+    from pathlib import Path
+    from fastreg_gb300 import estimate_inverse, interpolate_field
+    from oracle import ref_runner
+    f = np.load(Path(__file__).resolve().parent / "golden" / "field_ops.npz")
+    cases = {n: (f[f"{n}_psi"], f[f"{n}_psi_inv0"], f[f"{n}_field"], f[f"{n}_pos"])
+             for n in sorted({k.split("_")[0] for k in f.files})}
+    r = np.random.Generator(np.random.PCG64(9))
+    Z, Y, X = 7, 10, 15
+    zz, yy, xx = np.meshgrid(np.arange(Z), np.arange(Y), np.arange(X), indexing="ij")
+    idn = np.stack([xx, yy, zz]).astype(np.float32)
+    cen = np.array([(X - 1) / 2, (Y - 1) / 2, (Z - 1) / 2], np.float32).reshape(3, 1, 1, 1)
+    cases["random"] = ((-(cen + 0.4 * (idn - cen)) + r.normal(0, 0.6, idn.shape)).astype(np.float32), idn,
+                       r.normal(0, 1, idn.shape).astype(np.float32),
+                       (idn + r.uniform(-3, 3, idn.shape)).astype(np.float32))
+    for name, (psi, pinv0, field, pos) in cases.items():
+        for sweeps in (1, 48):
+            got = estimate_inverse(_to(cuda, psi), _to(cuda, pinv0.copy()), sweeps).cpu().numpy()
+            assert_bitexact(got, O.estimate_inverse(psi, pinv0, sweeps), f"estimate_inverse {name} x{sweeps}")
+            if sweeps == 48 and ref_runner.available():
+                assert_bitexact(got, ref_runner.estimate_inverse(psi, pinv0, 48), f"vs reference {name}")
+        got = interpolate_field(_to(cuda, field), _to(cuda, pos)).cpu().numpy()
+        assert_bitexact(got, O.interpolate_field(field, pos), f"interpolate_field {name}")
+        if ref_runner.available():
+            assert_bitexact(got, ref_runner.interpolate_gradient(field, pos), f"interpolate vs reference {name}")
