@@ -53,6 +53,7 @@ class fr_params(C.Structure):
         ("damping", C.c_float),
         ("step", C.c_float),
         ("keep_state", C.c_int),
+        ("autotune", C.c_int),
     ]
 
 
@@ -104,6 +105,7 @@ SIGNATURES = [
     ("fr_finish", C.c_int, [C.c_void_p, C.c_void_p]),
     ("fr_time_kernels", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     ("fr_warp", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fr_tile_shape", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("fr_estimate_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p]),
     ("fr_interpolate_field", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]),
     ("fr_sobolev_loss_grad", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_float, C.c_int,

@@ -22,8 +22,34 @@
 #include "fr_kernels.h"
 #include "fr_sob.h"
 
+#include <chrono>
+#include <map>
+#include <mutex>
+
 using frg::Pair;
 using frg::Tile;
+
+// The solver kernels and their tile tables.  Each kernel walks its own table of 32 x 8 x
+// depth tiles with a persistent grid of blocks_per_sm x SMs blocks (capped at the tile
+// count); the shape is the default below or the autotuner's choice.
+enum Role { R_LAP, R_PA, R_PB, R_SG, R_SS, R_SB, R_COUNT };
+struct Shape {
+    int depth = 16;  // slices per tile
+    int bps = 0;     // blocks per SM (0: the occupancy limit)
+};
+struct TileSet {
+    Shape shape;
+    std::vector<Tile> h;
+    Tile* d = nullptr;  // device copy (capacity cap tiles)
+    size_t cap = 0;
+    int occ = 1;   // resident blocks per SM at the kernel's registers and shared memory
+    int grid = 0;
+};
+// defaults, measured on the 182x218x182 pair: the depth that gives the persistent grid
+// the shortest tail (Laplacian 4, pass A 12 -- a tile also stages a 4-slice halo --,
+// pass B 8; the sobolev kernels 16)
+static const int kDefaultDepth[R_COUNT] = {4, 12, 8, 16, 16, 16};
+static const int kMinDepth = 4;
 
 struct fr_handle {
     fr_params P;
@@ -36,10 +62,9 @@ struct fr_handle {
     int npairs = 0;
     long long NT = 0;
     std::vector<Pair> hpairs;
-    std::vector<Tile> htiles;
-    // the reference solver's per-kernel tile tables (slices per tile kLapTileZ,
-    // kPassATileZ, kPassBTileZ)
-    std::vector<Tile> htiles_l, htiles_a, htiles_b;
+    std::vector<Tile> htiles;  // 32 x 8 x 16 tiles of the I/O kernels
+    TileSet ts[R_COUNT];       // the solver kernels' own tables
+    bool tuned = false;        // the shapes of this cohort are settled
     std::vector<fr_pair> io;  // caller buffers of the current registration
 
     // device memory
@@ -47,7 +72,6 @@ struct fr_handle {
     size_t block_bytes = 0;
     Pair* d_pairs = nullptr;
     Tile* d_tiles = nullptr;
-    Tile *d_tiles_l = nullptr, *d_tiles_a = nullptr, *d_tiles_b = nullptr;
     frg::PairIO* d_io = nullptr;
     float *S = nullptr, *T = nullptr;
     int16_t *labS = nullptr, *labT = nullptr;
@@ -69,8 +93,8 @@ struct fr_handle {
     float* grad = nullptr;  // unsmoothed gradient / smoothing temporaries (3 planes x 2)
     double* sob_energy = nullptr;
 
-    // launch shape
-    int grid_lap = 0, grid_a = 0, grid_b = 0, grid_io = 0;
+    // launch shape of the I/O kernels
+    int grid_io = 0;
 
     // graph of all iterations of a registration
     cudaStream_t cap_stream = nullptr;
@@ -186,6 +210,62 @@ void release(fr_handle* h) {
     h->have_state = false;
 }
 
+// ---- per-kernel tile tables ----
+std::vector<int> active_roles(const fr_handle* h) {
+    if (h->P.solver == FR_SOLVER_REFERENCE) return {R_LAP, R_PA, R_PB};
+    return {R_SG, R_SS, R_SB};
+}
+
+const void* role_fn(const fr_handle* h, int r) {
+    switch (r) {
+        case R_LAP: return (const void*)frg::ref_laplacian_kernel;
+        case R_PA: return (const void*)frg::ref_pass_a_kernel;
+        case R_PB: return (const void*)frg::ref_pass_b_kernel;
+        case R_SG: return (const void*)frg::sob_grad_kernel;
+        case R_SS: return frg::sob_smooth3_fn(h->P.smooth_width / 2);
+        default: return (const void*)frg::sob_pass_b_kernel;
+    }
+}
+
+size_t role_smem(int r) { return r == R_PA ? frg::ref_pass_a_smem_bytes() : 0; }
+
+typedef std::array<Shape, R_COUNT> Shapes;
+
+Shapes default_shapes(const fr_handle* h) {
+    Shapes sh{};
+    for (int r = 0; r < R_COUNT; ++r) sh[r] = Shape{kDefaultDepth[r], h->ts[r].occ};
+    return sh;
+}
+
+// table r with tiles of `depth` slices, copied to the device; grid = bps x SMs blocks
+int build_role(fr_handle* h, int r, Shape sh, cudaStream_t s = 0) {
+    TileSet& t = h->ts[r];
+    sh.depth = std::max(sh.depth, kMinDepth);
+    sh.bps = std::min(std::max(sh.bps, 1), t.occ);
+    t.shape = sh;
+    t.h.clear();
+    for (int p = 0; p < h->npairs; ++p) {
+        const Pair& P = h->hpairs[p];
+        for (int z0 = 0; z0 < P.Z; z0 += sh.depth)
+            for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
+                for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) t.h.push_back(make_int4(p, x0, y0, z0));
+    }
+    if (t.h.size() > t.cap) return fail(h, FR_ERR_STATE, "tile table %d overflows (%zu > %zu)", r, t.h.size(), t.cap);
+    FR_CUDA(h, cudaMemcpyAsync(t.d, t.h.data(), sizeof(Tile) * t.h.size(), cudaMemcpyHostToDevice, s));
+    FR_CUDA(h, cudaStreamSynchronize(s));  // t.h is rewritten by the next build
+    t.grid = (int)std::max(1LL, std::min<long long>((long long)sh.bps * h->num_sms, (long long)t.h.size()));
+    return FR_OK;
+}
+
+int apply_shapes(fr_handle* h, const Shapes& sh, cudaStream_t s = 0) {
+    for (int r : active_roles(h)) {
+        int rc = build_role(h, r, sh[r], s);
+        if (rc != FR_OK) return rc;
+    }
+    h->graph_valid = false;  // the captured launches carry the old tables
+    return FR_OK;
+}
+
 // (Re)build the packed cohort for the given pair sizes.
 int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     std::vector<std::array<int, 3>> dims(n);
@@ -208,14 +288,6 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     h->npairs = n;
     h->hpairs.assign(n, Pair{});
     h->htiles.clear();
-    h->htiles_l.clear();
-    h->htiles_a.clear();
-    h->htiles_b.clear();
-    auto column_tiles = [](std::vector<Tile>& dst, int p, const Pair& P, int depth) {
-        for (int z0 = 0; z0 < P.Z; z0 += depth)
-            for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
-                for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) dst.push_back(make_int4(p, x0, y0, z0));
-    };
     long long off = 0;
     for (int p = 0; p < n; ++p) {
         Pair& P = h->hpairs[p];
@@ -226,16 +298,9 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         P.N = (long long)P.Xp * P.Y * P.Z;
         P.off = off;
         off += (long long)align_up((size_t)P.N, 32);
-        const int tz = h->P.solver == FR_SOLVER_SOBOLEV ? frg::kSobTileZ : frg::kTileZ;
-        const int ty = h->P.solver == FR_SOLVER_SOBOLEV ? frg::kSobTileY : frg::kTileY;
-        for (int z0 = 0; z0 < P.Z; z0 += tz)
-            for (int y0 = 0; y0 < P.Y; y0 += ty)
+        for (int z0 = 0; z0 < P.Z; z0 += frg::kTileZ)  // the I/O kernels' table
+            for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
                 for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) h->htiles.push_back(make_int4(p, x0, y0, z0));
-        if (h->P.solver == FR_SOLVER_REFERENCE) {
-            column_tiles(h->htiles_l, p, P, frg::kLapTileZ);
-            column_tiles(h->htiles_a, p, P, frg::kPassATileZ);
-            column_tiles(h->htiles_b, p, P, frg::kPassBTileZ);
-        }
     }
     h->NT = std::max(off, 32LL);
     const long long NT = h->NT;
@@ -251,9 +316,15 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     auto add = [&](void** p, size_t bytes) { slots.push_back({p, bytes}); };
     add((void**)&h->d_pairs, sizeof(Pair) * n);
     add((void**)&h->d_tiles, sizeof(Tile) * ntiles);
-    add((void**)&h->d_tiles_l, sizeof(Tile) * std::max<size_t>(h->htiles_l.size(), 1));
-    add((void**)&h->d_tiles_a, sizeof(Tile) * std::max<size_t>(h->htiles_a.size(), 1));
-    add((void**)&h->d_tiles_b, sizeof(Tile) * std::max<size_t>(h->htiles_b.size(), 1));
+    // the solver kernels' tables, each with room for the shallowest tiles
+    size_t cap = 0;
+    for (const Pair& P : h->hpairs)
+        cap += (size_t)((P.X + frg::kTileX - 1) / frg::kTileX) * ((P.Y + frg::kTileY - 1) / frg::kTileY) *
+               ((P.Z + kMinDepth - 1) / kMinDepth);
+    for (int r : active_roles(h)) {
+        h->ts[r].cap = cap;
+        add((void**)&h->ts[r].d, sizeof(Tile) * cap);
+    }
     add((void**)&h->d_io, sizeof(frg::PairIO) * n);
     add((void**)&h->S, sizeof(float) * NT);
     add((void**)&h->T, sizeof(float) * NT);
@@ -305,23 +376,21 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     FR_CUDA(h, cudaMemset(h->block, 0, total));
     FR_CUDA(h, cudaMemcpy(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice));
     FR_CUDA(h, cudaMemcpy(h->d_tiles, h->htiles.data(), sizeof(Tile) * ntiles, cudaMemcpyHostToDevice));
-    for (auto tt : {std::make_pair(&h->htiles_l, h->d_tiles_l), std::make_pair(&h->htiles_a, h->d_tiles_a),
-                    std::make_pair(&h->htiles_b, h->d_tiles_b)})
-        if (!tt.first->empty())
-            FR_CUDA(h, cudaMemcpy(tt.second, tt.first->data(), sizeof(Tile) * tt.first->size(), cudaMemcpyHostToDevice));
-
-    if (h->P.solver == FR_SOLVER_REFERENCE) {
-        h->grid_lap = occupancy_grid(h, (const void*)frg::ref_laplacian_kernel, (int)h->htiles_l.size());
+    if (h->P.solver == FR_SOLVER_REFERENCE)
         FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)frg::ref_pass_a_smem_bytes()));
-        h->grid_a = occupancy_grid(h, (const void*)frg::ref_pass_a_kernel, (int)h->htiles_a.size(),
-                                   frg::ref_pass_a_smem_bytes());
-        h->grid_b = occupancy_grid(h, (const void*)frg::ref_pass_b_kernel, (int)h->htiles_b.size());
-    } else {
-        h->grid_a = occupancy_grid(h, (const void*)frg::sob_grad_kernel, ntiles);
-        h->grid_lap = occupancy_grid(h, frg::sob_smooth3_fn(h->P.smooth_width / 2), ntiles);
-        h->grid_b = occupancy_grid(h, (const void*)frg::sob_pass_b_kernel, ntiles);
+    for (int r : active_roles(h)) {
+        int occ = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, role_fn(h, r), 256, role_smem(r)) != cudaSuccess ||
+            occ < 1)
+            occ = 1;
+        h->ts[r].occ = occ;
+    }
+    h->tuned = false;
+    {
+        int rc = apply_shapes(h, default_shapes(h));
+        if (rc != FR_OK) return rc;
     }
     h->grid_io = occupancy_grid(h, (const void*)frg::finalize_kernel, ntiles);
     return FR_OK;
@@ -330,12 +399,15 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
 frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
     frg::RefIterArgs a{};
     a.pairs = h->d_pairs;
-    a.tiles_l = h->d_tiles_l;
-    a.ntiles_l = (int)h->htiles_l.size();
-    a.tiles_a = h->d_tiles_a;
-    a.ntiles_a = (int)h->htiles_a.size();
-    a.tiles_b = h->d_tiles_b;
-    a.ntiles_b = (int)h->htiles_b.size();
+    a.tiles_l = h->ts[R_LAP].d;
+    a.ntiles_l = (int)h->ts[R_LAP].h.size();
+    a.depth_l = h->ts[R_LAP].shape.depth;
+    a.tiles_a = h->ts[R_PA].d;
+    a.ntiles_a = (int)h->ts[R_PA].h.size();
+    a.depth_a = h->ts[R_PA].shape.depth;
+    a.tiles_b = h->ts[R_PB].d;
+    a.ntiles_b = (int)h->ts[R_PB].h.size();
+    a.depth_b = h->ts[R_PB].shape.depth;
     a.npairs = h->npairs;
     a.NT = h->NT;
     a.S = h->S;
@@ -370,11 +442,11 @@ frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
 int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev) {
     frg::RefIterArgs a = ref_args(h, iter, t);
     if (ev) cudaEventRecord(ev[0], s);
-    frg::ref_laplacian_kernel<<<h->grid_lap, 256, 0, s>>>(a);
+    frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    frg::ref_pass_a_kernel<<<h->grid_a, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
+    frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
-    frg::ref_pass_b_kernel<<<h->grid_b, 256, 0, s>>>(a);
+    frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);
     FR_LAUNCHED(h);
     return FR_OK;
@@ -383,12 +455,18 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
 // kernels launched per iteration
 int kernels_per_iter(const fr_handle* h) { return 3; }
 
-int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev = nullptr) {
-    if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
+frg::SobIterArgs sob_args(fr_handle* h, int iter) {
     frg::SobIterArgs a{};
     a.pairs = h->d_pairs;
-    a.tiles = h->d_tiles;
-    a.ntiles = (int)h->htiles.size();
+    a.tiles_g = h->ts[R_SG].d;
+    a.ntiles_g = (int)h->ts[R_SG].h.size();
+    a.depth_g = h->ts[R_SG].shape.depth;
+    a.tiles_s = h->ts[R_SS].d;
+    a.ntiles_s = (int)h->ts[R_SS].h.size();
+    a.depth_s = h->ts[R_SS].shape.depth;
+    a.tiles_b = h->ts[R_SB].d;
+    a.ntiles_b = (int)h->ts[R_SB].h.size();
+    a.depth_b = h->ts[R_SB].shape.depth;
     a.npairs = h->npairs;
     a.NT = h->NT;
     a.S = h->S;
@@ -408,7 +486,13 @@ int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev
     a.trace = h->trace;
     a.energy = h->sob_energy;
     a.counter = h->counter;
-    const int grids[3] = {h->grid_a, h->grid_lap, h->grid_b};
+    return a;
+}
+
+int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev = nullptr) {
+    if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
+    const frg::SobIterArgs a = sob_args(h, iter);
+    const int grids[3] = {h->ts[R_SG].grid, h->ts[R_SS].grid, h->ts[R_SB].grid};
     cudaError_t e = frg::launch_sob_iter(a, grids, s, ev);
     if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "sobolev launch failed: %s", cudaGetErrorString(e));
     return FR_OK;
@@ -567,6 +651,109 @@ int run_registration(fr_handle* h, cudaStream_t s) {
     return FR_OK;
 }
 
+// ---- autotuner ----
+// For each solver kernel, a few tile depths and blocks-per-SM counts are timed on the
+// freshly packed cohort (identity state, iteration 1), the kernel launched alone; the
+// fastest shape is kept.  The choice is cached per size class (solver, SM count,
+// smoothing width and the multiset of pair sizes) for the life of the process.  A tile
+// shape changes which block computes a voxel, never how, so results do not depend on it.
+std::string size_class(const fr_handle* h) {
+    std::ostringstream k;
+    k << h->P.solver << '/' << h->device << '/' << h->num_sms << '/'
+      << (h->P.solver == FR_SOLVER_SOBOLEV ? h->P.smooth_width : 0);
+    std::vector<std::array<int, 3>> d = h->dims;
+    std::sort(d.begin(), d.end());
+    for (const auto& x : d) k << '/' << x[0] << 'x' << x[1] << 'x' << x[2];
+    return k.str();
+}
+
+std::mutex g_tune_mu;
+std::map<std::string, Shapes> g_tuned;
+
+int launch_role(fr_handle* h, int r, float t, cudaStream_t s) {
+    frg::RefIterArgs ra{};
+    frg::SobIterArgs sa{};
+    void* args[1];
+    if (r == R_LAP || r == R_PA || r == R_PB) {
+        ra = ref_args(h, 1, t);
+        args[0] = &ra;
+    } else {
+        sa = sob_args(h, 1);
+        args[0] = &sa;
+    }
+    FR_CUDA(h, cudaLaunchKernel(role_fn(h, r), dim3(h->ts[r].grid), dim3(256), args, role_smem(r), s));
+    return FR_OK;
+}
+
+int autotune(fr_handle* h, cudaStream_t s) {
+    const std::string key = size_class(h);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tuned.find(key);
+        if (it != g_tuned.end()) {
+            int rc = apply_shapes(h, it->second, s);
+            if (rc == FR_OK) h->tuned = true;
+            return rc;
+        }
+    }
+    // a state to time on: the packed cohort of the current registration
+    FR_CUDA(h, cudaMemsetAsync(h->stop, 0, sizeof(int) * h->npairs, s));
+    frg::IoArgs io = io_args(h);
+    io.keep_state = 0;
+    frg::pack_init_kernel<<<h->grid_io, 256, 0, s>>>(io);
+    FR_LAUNCHED(h);
+    const float t = h->P.alpha;  // the first iteration's t
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FR_CUDA(h, cudaEventCreate(&e0));
+    FR_CUDA(h, cudaEventCreate(&e1));
+    Shapes best = default_shapes(h);
+    int rc = FR_OK;
+    for (int r : active_roles(h)) {
+        const int occ = h->ts[r].occ;
+        std::vector<int> bps = {occ};
+        if (occ > 1) bps.push_back(occ - 1);
+        if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
+        float best_ms = 1e30f;
+        for (int depth : {4, 8, 12, 16, 24}) {
+            for (int b : bps) {
+                rc = build_role(h, r, Shape{depth, b}, s);
+                if (rc != FR_OK) break;
+                if (cudaMemsetAsync(h->stop, 0, sizeof(int) * h->npairs, s) != cudaSuccess) {
+                    rc = fail(h, FR_ERR_CUDA, "autotune: memset failed");
+                    break;
+                }
+                rc = launch_role(h, r, t, s);  // warm-up
+                if (rc == FR_OK) cudaEventRecord(e0, s);
+                for (int k = 0; k < 3 && rc == FR_OK; ++k) rc = launch_role(h, r, t, s);
+                if (rc != FR_OK) break;
+                cudaEventRecord(e1, s);
+                if (cudaEventSynchronize(e1) != cudaSuccess) {
+                    rc = fail(h, FR_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best[r] = h->ts[r].shape;
+                }
+            }
+            if (rc != FR_OK) break;
+        }
+        if (rc != FR_OK) break;
+        rc = build_role(h, r, best[r], s);
+        if (rc != FR_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != FR_OK) return rc;
+    h->graph_valid = false;
+    h->tuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = best;
+    return FR_OK;
+}
+
 int begin(fr_handle* h, const fr_pair* pairs, int n, cudaStream_t s) {
     if (!pairs || n < 1) return fail(h, FR_ERR_INVALID_ARG, "need at least one pair");
     for (int p = 0; p < n; ++p)
@@ -586,6 +773,10 @@ int begin(fr_handle* h, const fr_pair* pairs, int n, cudaStream_t s) {
     std::vector<frg::PairIO> io(n);
     for (int p = 0; p < n; ++p) io[p] = frg::PairIO{pairs[p].img_T, pairs[p].lab_T, pairs[p].img_S, pairs[p].lab_S};
     FR_CUDA(h, cudaMemcpyAsync(h->d_io, io.data(), sizeof(frg::PairIO) * n, cudaMemcpyHostToDevice, s));
+    if (h->P.autotune && !h->tuned && !(h->P.keep_state && h->have_state)) {
+        rc = autotune(h, s);  // leaves the state to the initialisation below
+        if (rc != FR_OK) return rc;
+    }
     FR_CUDA(h, cudaMemsetAsync(h->stop, 0, sizeof(int) * n, s));
     FR_CUDA(h, cudaMemsetAsync(h->keys, 0, sizeof(unsigned long long) * n, s));
     FR_CUDA(h, cudaMemsetAsync(h->trace, 0, sizeof(unsigned long long) * n * (size_t)h->trace_cap, s));
@@ -703,6 +894,7 @@ int set_key(fr_params* p, const std::string& key, const std::string& val, std::s
     else if (key == "DAMPING") ok = as_float(&p->damping);
     else if (key == "STEP") ok = as_float(&p->step);
     else if (key == "KEEP_STATE") ok = as_int(&p->keep_state);
+    else if (key == "AUTOTUNE") ok = as_int(&p->autotune);
     else {
         *why = "unrecognised option '" + key + "'";
         return FR_ERR_PARSE;
@@ -778,6 +970,7 @@ int fr_params_default(fr_params* p) {
     p->damping = 0.9f;
     p->step = 0.5f;
     p->keep_state = 0;
+    p->autotune = 1;
     return FR_OK;
 }
 
@@ -1132,6 +1325,15 @@ static int field_op_launch(const void* fn, long long work, const char* who, void
         g_parse_error = std::string(who) + ": " + cudaGetErrorString(e);
         return FR_ERR_CUDA;
     }
+    return FR_OK;
+}
+
+int fr_tile_shape(const fr_handle* h, int k, int* depth, int* blocks_per_sm) {
+    if (!h || !depth || !blocks_per_sm || k < 0 || k > 2) return FR_ERR_INVALID_ARG;
+    if (!h->block) return FR_ERR_STATE;
+    const TileSet& t = h->ts[active_roles(h)[k]];
+    *depth = t.shape.depth;
+    *blocks_per_sm = t.shape.bps;
     return FR_OK;
 }
 

@@ -32,11 +32,9 @@ typedef int4 Tile;
 constexpr int kTileX = 32;  // threads along x (one warp per row)
 constexpr int kTileY = 8;   // rows per block
 constexpr int kTileZ = 16;  // slices marched by each thread
-// Slices per tile of each reference-mode kernel's own tile table: chosen so that the
-// persistent grids end with a short tail (a tile is the unit of work of one block)
-constexpr int kLapTileZ = 4;     // Laplacian
-constexpr int kPassATileZ = 12;  // pass A (each tile also stages a 4-slice halo)
-constexpr int kPassBTileZ = 8;   // pass B
+// The solver kernels walk their own tile tables of 32 x 8 x depth tiles; the depth of
+// each table and the kernel's blocks per SM are chosen on the host (fr_api.cu: defaults,
+// or the autotuner's choice for the cohort's size class).
 
 __device__ __forceinline__ long long lin(const Pair& P, int x, int y, int z) {
     return (long long)x + (long long)P.Xp * ((long long)y + (long long)P.Y * z);

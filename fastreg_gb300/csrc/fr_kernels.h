@@ -12,12 +12,12 @@ namespace frg {
 // Arguments of one reference-mode iteration (all three launches take the same block).
 struct RefIterArgs {
     const Pair* pairs;
-    const Tile* tiles_l;  // 32 x 8 x kLapTileZ tiles (Laplacian)
-    int ntiles_l;
-    const Tile* tiles_a;  // 32 x 8 x kPassATileZ tiles (pass A)
-    int ntiles_a;
-    const Tile* tiles_b;  // 32 x 8 x kPassBTileZ tiles (pass B)
-    int ntiles_b;
+    const Tile* tiles_l;  // 32 x 8 x depth_l tiles (Laplacian)
+    int ntiles_l, depth_l;
+    const Tile* tiles_a;  // 32 x 8 x depth_a tiles (pass A)
+    int ntiles_a, depth_a;
+    const Tile* tiles_b;  // 32 x 8 x depth_b tiles (pass B)
+    int ntiles_b, depth_b;
     int npairs;
     long long NT;  // packed voxels (plane stride of vector fields)
 

@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
         const float* __restrict__ Q2 = Q1 + a.NT;
         const float* __restrict__ T = a.T + P.off;
         float4* LT = a.LT + P.off;
-        const int z0 = max(tl.w, 1), z1 = min(tl.w + kLapTileZ, P.Z - 1);
+        const int z0 = max(tl.w, 1), z1 = min(tl.w + a.depth_l, P.Z - 1);
         for (int z = z0; z < z1; ++z) {
             const int i = x + X * y + XY * z;
             float l[3];
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
         const Pair P = a.pairs[tl.x];
         const int X = P.X, Y = P.Y, Z = P.Z, N = (int)P.N;
         const int Xp = P.Xp, XYp = P.Xp * P.Y;  // strides of the packed arrays
-        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + kPassATileZ, Z - 1);
+        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + a.depth_a, Z - 1);
         if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
         const long long NT = a.NT;
         const float* __restrict__ Vg[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
@@ -350,7 +350,7 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
             // the velocity pass A just wrote
             const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
             float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
-            const int z0 = max(tl.w, 1), z1 = min(tl.w + kPassBTileZ, P.Z - 1);
+            const int z0 = max(tl.w, 1), z1 = min(tl.w + a.depth_b, P.Z - 1);
             int i = x + Xp * y + XYp * z0;
             // psi of the next slice is loaded while this slice's gathers are in flight
             float nx = 0.f, ny = 0.f, nz = 0.f;

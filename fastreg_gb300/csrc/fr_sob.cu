@@ -51,8 +51,8 @@ __device__ __forceinline__ SobCell sob_locate(const Pair& P, float px, float py,
 
 __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
     __shared__ double red[32];
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_g; t += gridDim.x) {
+        const Tile tl = a.tiles_g[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
             float* g0 = a.g + P.off;
             float* g1 = g0 + NT;
             float* g2 = g1 + NT;
-            const int z1 = min(tl.w + kSobTileZ, P.Z);
+            const int z1 = min(tl.w + a.depth_g, P.Z);
             for (int z = tl.w; z < z1; ++z) {
                 const int i = x + X * y + XY * z;
                 const SobCell s = sob_locate(P, __ldg(phi0 + i), __ldg(phi1 + i), __ldg(phi2 + i));
@@ -139,15 +139,15 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
     __shared__ float Gx[2][3][H][kTileX];
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
 
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_s; t += gridDim.x) {
+        const Tile tl = a.tiles_s[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
         const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XY = P.Xp * P.Y;
         const long long NT = a.NT;
         const float* __restrict__ g0 = a.g + P.off;
         float* m[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
-        const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + kSobTileZ, Z);
+        const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + a.depth_s, Z);
         const int nsl = (zt1 - zt0) + 2 * R;
         const bool xedge = x0 - R < 0 || x0 + kTileX - 1 + R > X - 1;  // uniform over the block
 
@@ -258,8 +258,8 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
 __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
     __shared__ unsigned long long red[32];
     __shared__ bool last;
-    for (int t = blockIdx.x; t < a.ntiles; t += gridDim.x) {
-        const Tile tl = a.tiles[t];
+    for (int t = blockIdx.x; t < a.ntiles_b; t += gridDim.x) {
+        const Tile tl = a.tiles_b[t];
         if (a.stop[tl.x]) continue;
         const Pair P = a.pairs[tl.x];
         const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
             const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
             float* phi[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
             const float* __restrict__ mc[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
-            const int z1 = min(tl.w + kSobTileZ, P.Z);
+            const int z1 = min(tl.w + a.depth_b, P.Z);
             int i = x + X * y + XY * tl.w;
             // phi of the next slice is loaded while this slice's gathers are in flight
             float nx = phi[0][i], ny = phi[1][i], nz = phi[2][i];

@@ -22,14 +22,17 @@ namespace frg {
 
 constexpr int kMaxSmoothWidth = 15;
 constexpr int kSobTileY = 8;
-constexpr int kSobTileZ = 16;
-// the start/end kernels walk sobolev tiles with the reference tile extents
-static_assert(kSobTileY == kTileY && kSobTileZ == kTileZ, "tile extents must agree");
+static_assert(kSobTileY == kTileY, "tile extents must agree");
 
 struct SobIterArgs {
     const Pair* pairs;
-    const Tile* tiles;
-    int ntiles;
+    // each kernel's own table of 32 x 8 x depth tiles: gradient, smoothing, update
+    const Tile* tiles_g;
+    int ntiles_g, depth_g;
+    const Tile* tiles_s;
+    int ntiles_s, depth_s;
+    const Tile* tiles_b;
+    int ntiles_b, depth_b;
     int npairs;
     long long NT;
     const float* S;

@@ -37,6 +37,7 @@ class Params:
     damping: float = 0.9
     step: float = 0.5
     keep_state: int = 0
+    autotune: int = 1
 
     @classmethod
     def from_c(cls, c: N.fr_params) -> "Params":
@@ -46,7 +47,7 @@ class Params:
             alpha=c.alpha, p=c.p, C=c.C, reset_iter=c.reset_iter, verbosity=c.verbosity,
             solver="sobolev" if c.solver == N.FR_SOLVER_SOBOLEV else "reference",
             smooth_sigma=c.smooth_sigma, smooth_width=c.smooth_width, damping=c.damping, step=c.step,
-            keep_state=c.keep_state)
+            keep_state=c.keep_state, autotune=c.autotune)
 
     def to_c(self) -> N.fr_params:
         c = N.fr_params()
@@ -69,6 +70,7 @@ class Params:
         c.damping = float(self.damping)
         c.step = float(self.step)
         c.keep_state = int(self.keep_state)
+        c.autotune = int(self.autotune)
         return c
 
     @classmethod
@@ -238,6 +240,16 @@ class FastReg:
                 "fr_get_trace")
         m = min(n.value, cap)
         return norms[:m], vox[:m]
+
+    def tile_shapes(self):
+        """(slices per tile, blocks per SM) of the active solver's three kernels, in launch
+        order: the defaults or the autotuner's choice for this cohort."""
+        out = []
+        for k in range(3):
+            d, b = C.c_int(), C.c_int()
+            N.check(self.lib.fr_tile_shape(self.h, k, C.byref(d), C.byref(b)), self.h, "fr_tile_shape")
+            out.append((d.value, b.value))
+        return out
 
     # helpers
     def _pair_dims(self, pair, out):

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define FR_ABI_VERSION 1
+#define FR_ABI_VERSION 2
 
 /* status codes */
 #define FR_OK 0
@@ -67,6 +67,9 @@ typedef struct fr_params {
     float step;            /* STEP (sobolev step size) */
     int keep_state;        /* KEEP_STATE=1: continue from the previous call's fields,
                               as FastReg::operator() does on a reused instance */
+    int autotune;          /* AUTOTUNE=1 (default): time a few tile shapes and block counts
+                              per kernel on the first registration of a size class and
+                              keep the fastest (results do not depend on the shapes) */
 } fr_params;
 
 typedef struct fr_handle fr_handle;
@@ -139,6 +142,12 @@ int fr_finish(fr_handle *h, void *stream);                                  /* o
  *      0 gradient, 1 smoothing + momentum, 2 pass B);
  *      n_kernels receives the count.  No counterpart in the reference. ---- */
 int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *stream);
+
+/* Tile shape of kernel k (0..2: the active solver's kernels in launch order -- reference:
+ * Laplacian, pass A, pass B; sobolev: gradient, smoothing, update) after the last
+ * fr_register / fr_begin: slices per tile and blocks per SM, the defaults or the
+ * autotuner's choice (AUTOTUNE). */
+int fr_tile_shape(const fr_handle *h, int k, int *depth, int *blocks_per_sm);
 
 /* ---- standalone kernels of the hot path ---- */
 /* apply (vector_fields.cu:81-107): out = img o pos (trilinear), out_lab = lab at the floor

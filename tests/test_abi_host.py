@@ -41,7 +41,7 @@ def test_library_loads_and_exports_every_declared_symbol():
         getattr(lib, name)  # resolvable through ctypes
     # everything the ctypes binding wraps is declared
     assert {n for n, _, _ in N.SIGNATURES} <= decl
-    assert lib.fr_abi_version() == 1
+    assert lib.fr_abi_version() == 2
 
 
 REFERENCE_INI = """# IMAGES

@@ -87,3 +87,27 @@ def test_sobolev_smoothing_widths(cuda, width):
     o = O.sob_register(P, d["T"], d["S"])
     assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["phi"], f"phi (width {width})")
     assert_bitexact(fr.get_field(N.FR_FIELD_V).cpu().numpy(), o["m"], f"momentum (width {width})")
+
+
+@pytest.mark.parametrize("solver", ["reference", "sobolev"])
+def test_autotuned_shapes_do_not_change_results(cuda, solver):
+    """AUTOTUNE=1 times tile depths and blocks per SM per kernel and keeps the fastest;
+    the fields are bit-identical to AUTOTUNE=0's default shapes, and the chosen shapes
+    are among the candidates."""
+    dims_list = [(41, 23, 29), (20, 18, 16)]
+    kw = dict(no_labels=4, max_iter=12, alpha=0.02, solver=solver, step=0.5, damping=0.9)
+    pairs_np = [images(d, 700 + k) for k, d in enumerate(dims_list)]
+    fields = []
+    for tune in (0, 1):
+        fr = FastReg(Params(volume_dims=dims_list[0], autotune=tune, **kw))
+        bufs = [tuple(_to(cuda, p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+        fr.register_batch(bufs)
+        fields.append([fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy() for k in range(len(dims_list))])
+        shapes = fr.tile_shapes()
+        assert all(d in (4, 8, 12, 16, 24) and b >= 1 for d, b in shapes), shapes
+        if not tune:
+            default = (4, 12, 8) if solver == "reference" else (16, 16, 16)
+            assert tuple(d for d, _ in shapes) == default, shapes
+        fr.close()
+    for k in range(len(dims_list)):
+        assert_bitexact(fields[1][k], fields[0][k], f"pair {k} psi, autotuned vs default shapes")
