@@ -253,6 +253,33 @@ def adjoint_timing(dev, stream, reps=3):
             "loss": loss.value, "grad_lambda": gl.value}
 
 
+def small_pair_timing(dev, stream, reps=5):
+    """Registrations per second of the 64^3 pair (200 iterations), reference and sobolev
+    solvers, inputs resident; after warm-up registrations (which also tune the shapes)."""
+    import torch
+    from fastreg_gb300 import FastReg, synthetic as sy
+    d = sy.make_pair_torch(sy.CFG1, dev)
+    pristine = [d[k] for k in ("T", "labT", "S", "labS")]
+    work = [t.clone() for t in pristine]
+    out = {"dims": list(sy.CFG1.dims), "iterations": ITERS}
+    for solver in ("reference", "sobolev"):
+        fr = FastReg(reference_params(dims=sy.CFG1.dims, solver=solver))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            for rep in range(3 + reps):
+                if rep == 3:
+                    e0.record(stream)
+                for w, p in zip(work, pristine):
+                    w.copy_(p, non_blocking=True)
+                fr(*work, stream=stream, sync=False)
+            e1.record(stream)
+        stream.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[solver] = {"pairs_per_s": 1000.0 / ms, "ms_per_pair": ms, "tile_shapes": fr.tile_shapes()}
+        fr.close()
+    return out
+
+
 def batched_vs_plain(dev, stream, n_pairs=16, reps=2):
     """One fr_register_batch over the uneven cohort against one fr_register per pair
     (a handle per pair size), same data, same iterations; checks the two agree bit
@@ -515,6 +542,9 @@ def main():
                                                            data["S"].astype(np.float64)) ** 2).sum()),
                            "folds": ss.folds, "dice_all": ss.dice_all}
         frs.close()
+
+        # the 64^3 single-pair workload (the CPU-runnable configuration), both solvers
+        line["cfg1_64cube"] = small_pair_timing(dev, stream)
 
         # batched cohort against plain per-pair calls: 16 uneven pairs, 200 iterations each
         line["batched"] = batched_vs_plain(dev, stream)
