@@ -141,11 +141,8 @@ def barrier(ws):
 def allmax(ws, v):
     if ws == 1:
         return v
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from fastreg_gb300.replicas import max_over_ranks
+    return max_over_ranks(v)
 
 
 def cpu_reference_sample(data, P, sample_iters=(2, 6)):
