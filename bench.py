@@ -456,6 +456,8 @@ def main():
         "data": "synthetic (seeded: 400 Gaussian blobs + N(0,0.01), smooth velocity sigma 6, max disp 6, 8 classes)",
         "config": {"workload": "cfg2: one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
                    "solver": "reference", "voxels": int(np.prod(DIMS)), "iterations": ITERS,
+                   "other_solver": "the workload's Gaussian-smoothed (sobolev) settings -- width 7, sigma 1.5, "
+                                   "damping 0.9, step 0.5 -- are timed on the same pair in the 'sobolev' block",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "working set ~0.7 GB per pair, larger than L2 (no flush needed)"},
         "voxel_iters_per_s": value * int(np.prod(DIMS)) * ITERS,
