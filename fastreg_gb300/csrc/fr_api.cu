@@ -49,7 +49,7 @@ struct TileSet {
 // the shortest tail (Laplacian 4, pass A 12 -- a tile also stages a 4-slice halo --,
 // pass B 8; the sobolev kernels 16)
 static const int kDefaultDepth[R_COUNT] = {4, 12, 8, 16, 16, 16};
-static const int kMinDepth = 4;
+static const int kMinDepth = 1;  // thin tiles give small volumes enough blocks
 
 struct fr_handle {
     fr_params P;
@@ -714,7 +714,7 @@ int autotune(fr_handle* h, cudaStream_t s) {
         if (occ > 1) bps.push_back(occ - 1);
         if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
         float best_ms = 1e30f;
-        for (int depth : {4, 8, 12, 16, 24}) {
+        for (int depth : {1, 2, 4, 8, 12, 16, 24}) {
             for (int b : bps) {
                 rc = build_role(h, r, Shape{depth, b}, s);
                 if (rc != FR_OK) break;
