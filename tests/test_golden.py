@@ -9,7 +9,7 @@ resolution of the positions, and the check is:
   - psi, psi_inv, T o psi_inv, S o psi and both warped label maps: bit for bit;
   - the per-iteration max update norm (taken on the ~1e-5 voxel updates, where the
     differences in the velocity do show): <= 1e-6 relative, same voxel.
-The looser bounds of the spec contract (1e-5 relative on float fields; labels
+The looser bounds the path is held to (1e-5 relative on float fields; labels
 equal away from integer grid planes) are asserted as well, so a failure says which
 bound broke.
 """
