@@ -102,10 +102,11 @@ def cohort_dims(n_pairs: int, seed: int = 3000):
     return [(int(rng.choice(xs)), int(rng.choice(ys)), int(rng.choice(zs))) for _ in range(n_pairs)]
 
 
-def make_pair_torch(spec: PairSpec, device="cuda"):
+def make_pair_torch(spec: PairSpec, device="cuda", target=None, source_noise: float = 0.0):
     """The same construction on the GPU with torch (for large cohorts in the benchmark;
     the values differ from make_pair's in rounding).  Returns CUDA tensors T, labT, S,
-    labS of shape (Z, Y, X)."""
+    labS of shape (Z, Y, X).  With `target` (a (Z, Y, X) tensor) the blobs are skipped and
+    that target is warped; `source_noise` adds N(0, source_noise^2) to the source."""
     import torch
     import torch.nn.functional as F
 
@@ -118,7 +119,7 @@ def make_pair_torch(spec: PairSpec, device="cuda"):
     T = torch.zeros((Z, Y, X), device=dev, dtype=torch.float32)
     lo = torch.tensor([0.0, 0.0, 0.0])
     hi = torch.tensor([X - 1.0, Y - 1.0, Z - 1.0])
-    for _ in range(spec.n_blobs):
+    for _ in range(spec.n_blobs if target is None else 0):
         c = lo + (hi - lo) * torch.rand(3, generator=g)
         s = spec.sigma_range[0] + (spec.sigma_range[1] - spec.sigma_range[0]) * float(torch.rand(1, generator=g))
         a = spec.amp_range[0] + (spec.amp_range[1] - spec.amp_range[0]) * float(torch.rand(1, generator=g))
@@ -126,7 +127,9 @@ def make_pair_torch(spec: PairSpec, device="cuda"):
         T += a * (torch.exp(-(xx - float(c[0])) ** 2 * inv) * torch.exp(-(yy - float(c[1])) ** 2 * inv) *
                   torch.exp(-(zz - float(c[2])) ** 2 * inv))
     T = T.clamp(0.0, 1.0)
-    if spec.noise > 0:
+    if target is not None:
+        T = target.to(dev, torch.float32)
+    elif spec.noise > 0:
         T = T + spec.noise * torch.randn((Z, Y, X), generator=g).to(dev)
 
     def smooth(vol, sigma):
@@ -154,6 +157,8 @@ def make_pair_torch(spec: PairSpec, device="cuda"):
     for _ in range(spec.squarings):
         u = u + sample(u, u, "bilinear")
     S = sample(T[None], u, "bilinear")[0]
+    if source_noise > 0:
+        S = S + source_noise * torch.randn((Z, Y, X), generator=g).to(dev)
     thr = torch.arange(1, spec.n_classes, device=dev, dtype=torch.float32) / spec.n_classes
     labT = torch.bucketize(T.clamp(0.0, 1.0), thr, right=True).to(torch.int16)
     labS = sample(labT[None].float(), u, "nearest")[0].to(torch.int16)
@@ -170,3 +175,19 @@ def cohort_specs(n_pairs: int = 16, seed: int = 3000):
         specs.append(PairSpec(dims=d, n_blobs=max(40, n // 20000), vel_sigma=4.0,
                               max_disp=float(rng.uniform(2.0, 6.0)), n_classes=4, seed=seed + 100 + k))
     return specs
+
+
+def shared_target_cohort(n_pairs: int = 32, dims=(160, 192, 160), device="cuda", seed: int = 5000):
+    """The shared-target cohort: one target of Gaussian blobs; each source is that target
+    warped by its own seeded velocity (Gaussian sigma 5, maximum displacement 5 voxels)
+    plus N(0, 0.02) intensity noise; 8 label classes.  Returns a list of dicts as
+    make_pair_torch (the target tensors are shared)."""
+    n = dims[0] * dims[1] * dims[2]
+    base = PairSpec(dims=dims, n_blobs=max(40, n // 18000), vel_sigma=5.0, max_disp=5.0, n_classes=8, seed=seed)
+    first = make_pair_torch(base, device)
+    out = []
+    for k in range(n_pairs):
+        sp = PairSpec(**{**base.__dict__, "seed": seed + 1 + k})
+        d = make_pair_torch(sp, device, target=first["T"], source_noise=0.02)
+        out.append(d)
+    return out
