@@ -86,6 +86,8 @@ def test_params_ini_variant_keys_and_errors(tmp_path):
                              "KEEP_STATE=1\n[section]\n  MAX_ITER = 7  # comment\n")
     assert P.solver == "sobolev" and P.smooth_sigma == 2.0 and P.smooth_width == 9
     assert abs(P.damping - 0.8) < 1e-7 and P.step == 0.25 and P.keep_state == 1 and P.max_iter == 7
+    assert P.autotune == 1  # the default
+    assert Params.from_ini_text("AUTOTUNE=0\n").autotune == 0
     with pytest.raises(N.FastRegError) as e:
         Params.from_ini_text("NOT_A_KEY=1\n")
     assert e.value.status == N.FR_ERR_PARSE and "NOT_A_KEY" in str(e.value)
