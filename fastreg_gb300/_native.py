@@ -105,6 +105,7 @@ SIGNATURES = [
     ("fr_finish", C.c_int, [C.c_void_p, C.c_void_p]),
     ("fr_time_kernels", C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p]),
     ("fr_warp", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p]),
+    ("fr_set_pair_w_reg", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("fr_tile_shape", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     ("fr_estimate_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p]),
     ("fr_interpolate_field", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]),

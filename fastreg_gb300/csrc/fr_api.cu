@@ -66,6 +66,7 @@ struct fr_handle {
     TileSet ts[R_COUNT];       // the solver kernels' own tables
     bool tuned = false;        // the shapes of this cohort are settled
     std::vector<fr_pair> io;  // caller buffers of the current registration
+    std::vector<float> pair_w_reg;  // per-pair W_REG from fr_set_pair_w_reg (empty: P.w_reg)
 
     // device memory
     char* block = nullptr;
@@ -297,6 +298,7 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         P.Xp = (P.X + 3) / 4 * 4;  // rows on 16-byte boundaries
         P.N = (long long)P.Xp * P.Y * P.Z;
         P.off = off;
+        P.w_reg = h->P.w_reg;
         off += (long long)align_up((size_t)P.N, 32);
         for (int z0 = 0; z0 < P.Z; z0 += frg::kTileZ)  // the I/O kernels' table
             for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
@@ -569,8 +571,9 @@ int verbose_energy(fr_handle* h, int iter, cudaStream_t s, double* energy) {
     FR_CUDA(h, cudaMemcpyAsync(e.data(), h->pair_energy, sizeof(double) * 2 * h->npairs, cudaMemcpyDeviceToHost, s));
     FR_CUDA(h, cudaStreamSynchronize(s));
     for (int p = 0; p < h->npairs; ++p) {
-        double val = e[2 * p] + (double)h->P.w_reg * e[2 * p + 1];
-        printf("data energy + w_reg * reg energy = %g + %g * %g = %g\n", e[2 * p], (double)h->P.w_reg, e[2 * p + 1],
+        const double w = h->hpairs[p].w_reg;
+        double val = e[2 * p] + w * e[2 * p + 1];
+        printf("data energy + w_reg * reg energy = %g + %g * %g = %g\n", e[2 * p], w, e[2 * p + 1],
                val);
         if (p == 0) *energy = val;
     }
@@ -766,9 +769,23 @@ int begin(fr_handle* h, const fr_pair* pairs, int n, cudaStream_t s) {
         int rc = normalise_parity(h);
         if (rc != FR_OK) return rc;
     }
+    if (!h->pair_w_reg.empty() && (int)h->pair_w_reg.size() != n)
+        return fail(h, FR_ERR_INVALID_ARG, "fr_set_pair_w_reg gave %zu weights for a cohort of %d pairs",
+                    h->pair_w_reg.size(), n);
     int rc = setup_cohort(h, pairs, n);
     if (rc != FR_OK) return rc;
     if (!same) h->have_state = false;
+    {  // each pair's regularisation weight (read by the kernels from the pair table)
+        bool changed = false;
+        for (int p = 0; p < n; ++p) {
+            const float w = h->pair_w_reg.empty() ? h->P.w_reg : h->pair_w_reg[p];
+            if (h->hpairs[p].w_reg != w) {
+                h->hpairs[p].w_reg = w;
+                changed = true;
+            }
+        }
+        if (changed) FR_CUDA(h, cudaMemcpyAsync(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice, s));
+    }
     h->io.assign(pairs, pairs + n);
     std::vector<frg::PairIO> io(n);
     for (int p = 0; p < n; ++p) io[p] = frg::PairIO{pairs[p].img_T, pairs[p].lab_T, pairs[p].img_S, pairs[p].lab_S};
@@ -829,7 +846,7 @@ int host_stats(fr_handle* h) {
         }
         st.e_data = energy[2 * p];
         st.e_reg = energy[2 * p + 1];
-        st.energy = st.e_data + (double)h->P.w_reg * st.e_reg;
+        st.energy = st.e_data + (double)h->hpairs[p].w_reg * st.e_reg;
         st.folds = folds[p];
         st.no_labels = h->P.no_labels;
         const unsigned long long* dp = dice.data() + (size_t)p * (2 * 256 + 1);
@@ -1325,6 +1342,19 @@ static int field_op_launch(const void* fn, long long work, const char* who, void
         g_parse_error = std::string(who) + ": " + cudaGetErrorString(e);
         return FR_ERR_CUDA;
     }
+    return FR_OK;
+}
+
+int fr_set_pair_w_reg(fr_handle* h, const float* w_reg, int n) {
+    if (!h) return FR_ERR_INVALID_ARG;
+    h->err.clear();
+    if (!w_reg || n <= 0) {
+        h->pair_w_reg.clear();
+        return FR_OK;
+    }
+    for (int p = 0; p < n; ++p)
+        if (!std::isfinite(w_reg[p])) return fail(h, FR_ERR_INVALID_ARG, "w_reg[%d] is not finite", p);
+    h->pair_w_reg.assign(w_reg, w_reg + n);
     return FR_OK;
 }
 

@@ -24,6 +24,8 @@ struct Pair {
     int Xp;         // row pitch in the packed arrays (X rounded up to a multiple of 4)
     long long off;  // voxel offset into the packed arrays
     long long N;    // Xp*Y*Z: the pair's extent in the packed arrays
+    float w_reg;    // regularisation weight of this pair (W_REG unless set per pair)
+    int pad_;
 };
 
 // A tile of work: pair index and the tile origin (x0, y0, z0).

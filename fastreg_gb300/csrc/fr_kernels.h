@@ -33,7 +33,7 @@ struct RefIterArgs {
     float* psi;         // psi (in place)
     float4* LT;         // (-Laplacian(psi), T) interleaved: the two fields pass A gathers at psi_inv
 
-    float alpha, f1, m2, tau, w_reg, max_update_norm;
+    float alpha, f1, m2, tau, w_reg, max_update_norm;  // w_reg: W_REG (pass A uses Pair::w_reg)
     int iter;        // 1-based iteration number
     int first_iter;  // T o psi_inv is T itself on the first iteration of a call
 

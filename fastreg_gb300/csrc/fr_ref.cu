@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                 const float diff = Si - Tq;
                 float gU[3];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (a.w_reg * Lq[c])) * det;
+                for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (P.w_reg * Lq[c])) * det;
 
                 // velocity and its 6 neighbours (vb[2] is slice z)
                 float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];

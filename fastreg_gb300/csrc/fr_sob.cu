@@ -104,9 +104,9 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                     }
                     lap[c] = acc;
                 }
-                g0[i] = (r * dWa) + (a.lambda * lap[0]);
-                g1[i] = (r * dWb) + (a.lambda * lap[1]);
-                g2[i] = (r * dWc) + (a.lambda * lap[2]);
+                g0[i] = (r * dWa) + (P.w_reg * lap[0]);
+                g1[i] = (r * dWb) + (P.w_reg * lap[1]);
+                g2[i] = (r * dWc) + (P.w_reg * lap[2]);
                 e += (double)r * (double)r;
             }
         }

@@ -41,7 +41,7 @@ struct SobIterArgs {
     float* m;     // momentum (3 planes)
     float* g;     // gradient (3 planes)
     float damping, step;
-    float lambda;  // weight of the displacement's graph Laplacian (W_REG)
+    float lambda;  // W_REG; the kernels take each pair's weight from Pair::w_reg
     float taps[kMaxSmoothWidth];
     int radius;
     float max_update_norm;

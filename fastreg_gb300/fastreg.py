@@ -241,6 +241,15 @@ class FastReg:
         m = min(n.value, cap)
         return norms[:m], vox[:m]
 
+    def set_pair_w_reg(self, weights=None) -> None:
+        """Per-pair W_REG for the next cohorts (one weight per pair, in order); None goes
+        back to params.w_reg."""
+        if weights is None:
+            N.check(self.lib.fr_set_pair_w_reg(self.h, None, 0), self.h, "fr_set_pair_w_reg")
+            return
+        w = (C.c_float * len(weights))(*[float(v) for v in weights])
+        N.check(self.lib.fr_set_pair_w_reg(self.h, w, len(weights)), self.h, "fr_set_pair_w_reg")
+
     def tile_shapes(self):
         """(slices per tile, blocks per SM) of the active solver's three kernels, in launch
         order: the defaults or the autotuner's choice for this cohort."""

@@ -143,6 +143,13 @@ int fr_finish(fr_handle *h, void *stream);                                  /* o
  *      n_kernels receives the count.  No counterpart in the reference. ---- */
 int fr_time_kernels(fr_handle *h, int iters, float *ms, int *n_kernels, void *stream);
 
+/* Per-pair regularisation weights (W_REG) for the cohorts registered from now on: w_reg[p]
+ * for pair p of the next fr_register_batch / fr_begin, which must have n pairs; NULL or
+ * n <= 0 goes back to params.w_reg for every pair.  (The reference has one W_REG per
+ * FastReg; this lets one batched launch register pairs with their own weights, e.g. each
+ * tuned by fr_sobolev_loss_grad.) */
+int fr_set_pair_w_reg(fr_handle *h, const float *w_reg, int n);
+
 /* Tile shape of kernel k (0..2: the active solver's kernels in launch order -- reference:
  * Laplacian, pass A, pass B; sobolev: gradient, smoothing, update) after the last
  * fr_register / fr_begin: slices per tile and blocks per SM, the defaults or the

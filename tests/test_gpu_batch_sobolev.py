@@ -111,3 +111,39 @@ def test_autotuned_shapes_do_not_change_results(cuda, solver):
         fr.close()
     for k in range(len(dims_list)):
         assert_bitexact(fields[1][k], fields[0][k], f"pair {k} psi, autotuned vs default shapes")
+
+
+@pytest.mark.parametrize("solver", ["reference", "sobolev"])
+def test_per_pair_w_reg(cuda, solver):
+    """fr_set_pair_w_reg: one batched registration with a regularisation weight per pair
+    gives, pair by pair, the oracle's bits for that pair's W_REG; the energy uses it."""
+    dims_list = [(20, 18, 16), (33, 17, 21), (16, 24, 12)]
+    weights = [0.05, 0.2, 0.6]
+    kw = dict(no_labels=4, max_iter=20, alpha=0.02, solver=solver, step=0.5, damping=0.9)
+    pairs_np = [images(d, 900 + k) for k, d in enumerate(dims_list)]
+    fr = FastReg(Params(volume_dims=dims_list[0], w_reg=0.3, **kw))
+    fr.set_pair_w_reg(weights)
+    bufs = [tuple(_to(cuda, p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+    fr.register_batch(bufs)
+    for k, (d, p) in enumerate(zip(dims_list, pairs_np)):
+        Pk = Params(volume_dims=d, w_reg=weights[k], **kw)
+        psi = fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy()
+        if solver == "reference":
+            o = O.ref_register(Pk, p["T"], p["labT"], p["S"], p["labS"])
+            assert_bitexact(psi, o["psi"], f"pair {k} psi (w_reg {weights[k]})")
+        else:
+            o = O.sob_register(Pk, p["T"], p["S"])
+            assert_bitexact(psi, o["phi"], f"pair {k} phi (w_reg {weights[k]})")
+        st = fr.stats(pair=k)
+        assert abs(st.energy - (st.e_data + float(np.float32(weights[k])) * st.e_reg)) <= 1e-12 * abs(st.energy)
+    fr.set_pair_w_reg([0.1])  # one weight for three pairs
+    with pytest.raises(N.FastRegError):
+        fr.register_batch(bufs)
+    fr.set_pair_w_reg(None)  # back to W_REG = 0.3 for every pair
+    fr.register_batch([tuple(_to(cuda, pairs_np[0][k]) for k in ("T", "labT", "S", "labS"))])  # fresh inputs
+    o = (O.ref_register(Params(volume_dims=dims_list[0], w_reg=0.3, **kw), *(pairs_np[0][k] for k in
+                                                                                ("T", "labT", "S", "labS")))
+         if solver == "reference" else O.sob_register(Params(volume_dims=dims_list[0], w_reg=0.3, **kw),
+                                                       pairs_np[0]["T"], pairs_np[0]["S"]))
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi" if solver == "reference" else "phi"], "W_REG")
+    fr.close()
