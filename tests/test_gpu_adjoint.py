@@ -138,3 +138,30 @@ def test_warp_adjoint(cuda):
     pb64, ib64 = O.warp_adjoint(pos, img, wbar)
     assert np.abs(pb.cpu().numpy() - pb64).max() <= 1e-5 * max(1.0, np.abs(pb64).max())
     assert np.abs(ib.cpu().numpy() - ib64).max() <= 1e-5 * max(1.0, np.abs(ib64).max())
+
+
+def test_hypergradient_tuned_cohort(cuda):
+    """fastreg_gb300.hypertune: per-pair W_REG from hypergradient steps through short
+    unrolled registrations, then one batched registration with those weights -- the same
+    bits as each pair registered alone with its weight."""
+    import torch
+    from fastreg_gb300 import FastReg, Params, _native as N
+    from fastreg_gb300.hypertune import register_cohort_tuned, tune_w_reg
+    dims_list = [(24, 20, 18), (20, 22, 16)]
+    pairs_np = [images(d, 1200 + k) for k, d in enumerate(dims_list)]
+    kw = dict(no_labels=4, max_iter=15, solver="sobolev", smooth_sigma=1.5, smooth_width=7, damping=0.9, step=0.5,
+              w_reg=0.2)
+    P = Params(volume_dims=dims_list[0], **kw)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(cuda)  # noqa: E731
+    lam, hist = tune_w_reg(t(pairs_np[0]["T"]), t(pairs_np[0]["S"]), P, steps=2, iters=5, checkpoint_every=2)
+    assert len(hist) == 2 and all(np.isfinite(h[1]) and np.isfinite(h[2]) for h in hist)
+    assert lam > 0 and np.isfinite(lam) and lam != 0.2
+    fr = FastReg(P)
+    work = [tuple(t(p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+    weights = register_cohort_tuned(fr, work, P, steps=2, iters=5, checkpoint_every=2)
+    for k, (d, p) in enumerate(zip(dims_list, pairs_np)):
+        alone = FastReg(Params(volume_dims=d, **{**kw, "w_reg": float(np.float32(weights[k]))}))
+        alone(*(t(p[q]) for q in ("T", "labT", "S", "labS")))
+        assert torch.equal(fr.get_field(N.FR_FIELD_PSI, pair=k), alone.get_field(N.FR_FIELD_PSI)), k
+        alone.close()
+    fr.close()
