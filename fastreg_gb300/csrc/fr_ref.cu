@@ -73,30 +73,31 @@ __device__ __forceinline__ float entropy_flux(float c, float n) {
 // ----------------------------------------------------------------------------------
 // fused pass A
 //
-// A block owns a 32 x 8 column tile and marches z.  The vector stencil operands (v with
-// a 2-voxel halo and a 5-slice window; psi_inv with a 1-voxel halo and a 3-slice window)
-// are staged in shared-memory ring buffers by cp.async kAhead slices ahead of the
-// compute, so their 40 stencil reads per voxel are shared-memory loads and the global
-// traffic is one coalesced pass per field; the scalar stencils (rho, S) go through L1.
-// T o psi_inv and L o psi_inv are gathered from the interleaved LT field (eight 16-byte
-// loads per voxel).  The LT rows of the next slice's cell and the rho/S slice three steps
-// ahead are prefetched into L2 (7% faster than without: the kernel is latency-bound).
+// A block owns a 32 x 8 column tile and marches z.  Every stencil operand is staged in
+// shared-memory ring buffers by 16-byte cp.async one slice ahead of the compute: v with
+// a 2-voxel halo over a 5-slice window, and psi_inv, rho and S with a 1-voxel halo over a
+// 3-slice window (one ring of five components), so the stencil reads are shared-memory
+// loads and the global traffic is one coalesced pass per field.  T o psi_inv and
+// L o psi_inv are gathered from the interleaved LT field (eight 16-byte loads per voxel).
+// The LT rows of the next slice's cell and the rho/S slice three steps ahead are
+// prefetched into L2 (the kernel is latency-bound).
 // ----------------------------------------------------------------------------------
 namespace {
 // prefetch distance: slices in flight ahead of the one being computed
-constexpr int kAhead = 2;
+constexpr int kAhead = 1;
 // Staged rows cover x0 - 4 .. x0 + 35 (ten aligned 16-byte chunks): column x0 + tx sits
 // at row offset tx + kXO.  v has a 2-row y halo, psi_inv a 1-row one.
 constexpr int kXO = 4, kChunks = (kTileX + 2 * kXO) / 4;
 constexpr int kVH = 2, kVW = kTileX + 2 * kXO, kVR = kTileY + 2 * kVH, kVS = 5 + kAhead;  // v: halo, width, rows, slots
 constexpr int kQH = 1, kQW = kTileX + 2 * kXO, kQR = kTileY + 2 * kQH, kQS = 3 + kAhead;  // psi_inv
 constexpr int kVPlane = kVW * kVR, kQPlane = kQW * kQR;
-constexpr int kPassASmemFloats = 3 * kVS * kVPlane + 3 * kQS * kQPlane;  // v x3, psi_inv x3
+constexpr int kQC = 5;  // the psi_inv ring also holds rho and S (same halo and window)
+constexpr int kPassASmemFloats = 3 * kVS * kVPlane + kQC * kQS * kQPlane;  // v x3, psi_inv x3, rho, S
 constexpr size_t kPassASmemBytes = sizeof(float) * kPassASmemFloats;
 
 struct PassASmem {
     float* v;  // [3][kVS][kVR][kVW]
-    float* q;  // [3][kQS][kQR][kQW]
+    float* q;  // [kQC][kQS][kQR][kQW]: psi_inv x, y, z, rho, S
 };
 
 // A staged slice of a plane with y halo H is R = 8 + 2H rows (y0 - H .. y0 + 7 + H) of
@@ -159,12 +160,14 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) cp_async16(dst + c * kVS * kVPlane, Vg[c] + off);
         };
-        auto stage_q = [&](int zs) {  // slice zs of psi_inv's three components
+        auto stage_q = [&](int zs) {  // slice zs of psi_inv's three components, rho and S
             if (gq < 0 || zs < 0 || zs >= Z) return;
             float* dst = sm.q + qslot(zs) * kQPlane + 4 * threadIdx.x;
             const int off = gq + XYp * zs;
 #pragma unroll
             for (int c = 0; c < 3; ++c) cp_async16(dst + c * kQS * kQPlane, Qg[c] + off);
+            cp_async16(dst + 3 * kQS * kQPlane, Rg + off);
+            cp_async16(dst + 4 * kQS * kQPlane, Sg + off);
         };
 
         __syncthreads();  // the previous tile is done with the ring buffers
@@ -202,13 +205,13 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 #pragma unroll
                     for (int c = 0; c < 3; ++c) vb[k][c] = sm.v + (c * kVS + sl) * kVPlane + vc0;
                 }
-                const float* qb[3][3];
+                const float* qb[3][kQC];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     int sl = sq + k;
                     sl = sl >= kQS ? sl - kQS : sl;
 #pragma unroll
-                    for (int c = 0; c < 3; ++c) qb[k][c] = sm.q + (c * kQS + sl) * kQPlane + qc0;
+                    for (int c = 0; c < kQC; ++c) qb[k][c] = sm.q + (c * kQS + sl) * kQPlane + qc0;
                 }
 
                 // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
@@ -234,14 +237,14 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 
                 // central-difference gradient of S and the potential gradient
                 // rho and S are read through L1 (their 7-point stencils stay in cache)
-                const float Si = __ldg(Sg + i);
+                const float Si = qb[1][4][0];
                 if (z + 3 < Z) {  // the S and rho slice this column reads three steps on
                     prefetch_l2(Sg + i + 3 * XYp);
                     prefetch_l2(Rg + i + 3 * XYp);
                 }
-                const float gs[3] = {(__ldg(Sg + i + 1) - __ldg(Sg + i - 1)) * 0.5f,
-                                     (__ldg(Sg + i + Xp) - __ldg(Sg + i - Xp)) * 0.5f,
-                                     (__ldg(Sg + i + XYp) - __ldg(Sg + i - XYp)) * 0.5f};
+                const float gs[3] = {(qb[1][4][1] - qb[1][4][-1]) * 0.5f,
+                                     (qb[1][4][kQW] - qb[1][4][-kQW]) * 0.5f,
+                                     (qb[2][4][0] - qb[0][4][0]) * 0.5f};
                 const float diff = Si - Tq;
                 float gU[3];
 #pragma unroll
@@ -262,13 +265,14 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
                 const float vx = vc[0], vy = vc[1], vz = vc[2];
 
                 // divergence of rho*v (upwind) and the density update
-                const float p = __ldg(Rg + i);
-                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * __ldg(Rg + i + 1);
-                const float t12 = (vxm[0] > 0.f) ? vxm[0] * __ldg(Rg + i - 1) : vxm[0] * p;
-                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * __ldg(Rg + i + Xp);
-                const float t22 = (vym[1] > 0.f) ? vym[1] * __ldg(Rg + i - Xp) : vym[1] * p;
-                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * __ldg(Rg + i + XYp);
-                const float t32 = (vzm[2] > 0.f) ? vzm[2] * __ldg(Rg + i - XYp) : vzm[2] * p;
+                const float* rb = qb[1][3];
+                const float p = rb[0];
+                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * rb[1];
+                const float t12 = (vxm[0] > 0.f) ? vxm[0] * rb[-1] : vxm[0] * p;
+                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * rb[kQW];
+                const float t22 = (vym[1] > 0.f) ? vym[1] * rb[-kQW] : vym[1] * p;
+                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * qb[2][3][0];
+                const float t32 = (vzm[2] > 0.f) ? vzm[2] * qb[0][3][0] : vzm[2] * p;
                 const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
                 const float rho_new = p + a.alpha * div;
                 rho_n[i] = rho_new;
