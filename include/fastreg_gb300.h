@@ -152,8 +152,8 @@ int fr_set_pair_w_reg(fr_handle *h, const float *w_reg, int n);
 
 /* Tile shape of kernel k (0..2: the active solver's kernels in launch order -- reference:
  * Laplacian, pass A, pass B; sobolev: gradient, smoothing, update) after the last
- * fr_register / fr_begin: slices per tile and blocks per SM, the defaults or the
- * autotuner's choice (AUTOTUNE). */
+ * fr_register / fr_begin: slices per tile and blocks per SM (-1: one block per tile),
+ * the defaults or the autotuner's choice (AUTOTUNE). */
 int fr_tile_shape(const fr_handle *h, int k, int *depth, int *blocks_per_sm);
 
 /* ---- standalone kernels of the hot path ---- */

@@ -104,9 +104,9 @@ def test_autotuned_shapes_do_not_change_results(cuda, solver):
         fr.register_batch(bufs)
         fields.append([fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy() for k in range(len(dims_list))])
         shapes = fr.tile_shapes()
-        assert all(d in (1, 2, 4, 8, 12, 16, 24) and b >= 1 for d, b in shapes), shapes
+        assert all(d in (1, 2, 4, 8, 12, 16, 24, 32, 48) and (b >= 1 or b == -1) for d, b in shapes), shapes
         if not tune:
-            default = (4, 12, 8) if solver == "reference" else (16, 16, 16)
+            default = (4, 24, 24) if solver == "reference" else (16, 32, 8)
             assert tuple(d for d, _ in shapes) == default, shapes
         fr.close()
     for k in range(len(dims_list)):
