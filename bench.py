@@ -198,8 +198,34 @@ def run_reference_arm(args):
 def profile_case(args):
     """The bench workload for ncu captures: one registration that settles the tile shapes
     (the autotuner's launches), then the profiled registration and warp inside the NVTX
-    range "profile" (capture with --nvtx --nvtx-include "profile/")."""
+    range "profile" (capture with --nvtx --nvtx-include "profile/").  With --solver adjoint:
+    the differentiated registration of the 128^3 pair (--iters unrolled iterations,
+    checkpoints every 10), once outside and once inside the range."""
     import torch
+    if args.solver == "adjoint":
+        import ctypes as C
+        from fastreg_gb300 import synthetic as sy, _native as N
+        lib = N.load()
+        dev = torch.device("cuda", 0)
+        d = sy.make_pair_torch(sy.PairSpec(dims=(128, 128, 128), n_blobs=40, vel_sigma=4.0, max_disp=4.0,
+                                           n_classes=4, seed=4000), dev)
+        v0 = (0.05 * torch.randn((3, 128, 128, 128), generator=torch.Generator().manual_seed(4001))).to(dev)
+        gv = torch.empty_like(v0)
+        P = reference_params(dims=(128, 128, 128), solver="sobolev")
+        dims = (C.c_int * 3)(128, 128, 128)
+        loss, gl = C.c_double(), C.c_double()
+        for rep in range(2):
+            if rep:
+                torch.cuda.synchronize()
+                torch.cuda.nvtx.range_push("profile")
+            N.check(lib.fr_sobolev_loss_grad(d["T"].data_ptr(), d["S"].data_ptr(), dims, v0.data_ptr(), 0.2,
+                                             args.iters, 10, P.damping, P.step, P.smooth_sigma, P.smooth_width,
+                                             C.byref(loss), gv.data_ptr(), C.byref(gl), None), None,
+                    "fr_sobolev_loss_grad")
+            torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+        print(f"profile case: adjoint, {args.iters} iterations, J {loss.value:.6g}, dJ/dlambda {gl.value:.6g}")
+        return 0
     from fastreg_gb300 import FastReg, synthetic as sy, warp, _native as N
     dev = torch.device("cuda", 0)
     data = sy.make_pair(sy.CFG2)
@@ -426,7 +452,7 @@ def main():
                     help="one registration of the bench pair with --iters iterations and one standalone warp, "
                          "for ncu (no timing, no JSON line)")
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations of the --profile registration")
-    ap.add_argument("--solver", default="reference", choices=["reference", "sobolev"],
+    ap.add_argument("--solver", default="reference", choices=["reference", "sobolev", "adjoint"],
                     help="solver of the --profile registration")
     args = ap.parse_args()
     if args.profile:
