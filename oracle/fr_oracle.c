@@ -707,31 +707,40 @@ double FN(sob_grad)(const int *dims, const real *S, const real *T, const real *p
                     real *W_out) {
     fro_dims d = {dims[0], dims[1], dims[2]};
     const int64_t N = nvox(&d), X = d.X, XY = (int64_t)d.X * d.Y;
-    double e = 0.0;
-    for (int64_t i = 0; i < N; ++i) {
-        fro_scell s;
-        sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
-        const int64_t b = s.base;
-        const real f000 = S[b], f100 = S[b + 1], f010 = S[b + X], f110 = S[b + 1 + X];
-        const real f001 = S[b + XY], f101 = S[b + 1 + XY], f011 = S[b + X + XY], f111 = S[b + 1 + X + XY];
-        const real e11 = lerp_(f111, f110, s.c), e10 = lerp_(f101, f100, s.c);
-        const real e01 = lerp_(f011, f010, s.c), e00 = lerp_(f001, f000, s.c);
-        const real A1 = lerp_(e11, e10, s.b), A0 = lerp_(e01, e00, s.b);
-        const real W = lerp_(A1, A0, s.a);
-        const real dWa = s.in_x ? A1 - A0 : R(0);
-        const real dWb = s.in_y ? lerp_(e11 - e10, e01 - e00, s.a) : R(0);
-        const real dWc = s.in_z ? lerp_(lerp_(f111 - f110, f101 - f100, s.b), lerp_(f011 - f010, f001 - f000, s.b), s.a)
-                                : R(0);
-        const real r = W - T[i];
-        const int z = (int)(i / XY), y = (int)((i - z * XY) / X), x = (int)(i - z * XY - y * X);
-        real lap[3];
-        lap_u_(&d, phi, x, y, z, lap);
-        g[i] = (r * dWa) + (lambda * lap[0]);
-        g[N + i] = (r * dWb) + (lambda * lap[1]);
-        g[2 * N + i] = (r * dWc) + (lambda * lap[2]);
-        if (W_out) W_out[i] = W;
-        e += (double)r * (double)r;
+    /* per-slice partial sums added in slice order: the same energy for any thread count */
+    double *part = (double *)calloc((size_t)d.Z, sizeof(double));
+#pragma omp parallel for schedule(static)
+    for (int zz = 0; zz < d.Z; ++zz) {
+        double ez = 0.0;
+        for (int64_t i = zz * XY; i < (zz + 1) * XY; ++i) {
+            fro_scell s;
+            sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
+            const int64_t b = s.base;
+            const real f000 = S[b], f100 = S[b + 1], f010 = S[b + X], f110 = S[b + 1 + X];
+            const real f001 = S[b + XY], f101 = S[b + 1 + XY], f011 = S[b + X + XY], f111 = S[b + 1 + X + XY];
+            const real e11 = lerp_(f111, f110, s.c), e10 = lerp_(f101, f100, s.c);
+            const real e01 = lerp_(f011, f010, s.c), e00 = lerp_(f001, f000, s.c);
+            const real A1 = lerp_(e11, e10, s.b), A0 = lerp_(e01, e00, s.b);
+            const real W = lerp_(A1, A0, s.a);
+            const real dWa = s.in_x ? A1 - A0 : R(0);
+            const real dWb = s.in_y ? lerp_(e11 - e10, e01 - e00, s.a) : R(0);
+            const real dWc = s.in_z ? lerp_(lerp_(f111 - f110, f101 - f100, s.b), lerp_(f011 - f010, f001 - f000, s.b), s.a)
+                                    : R(0);
+            const real r = W - T[i];
+            const int z = (int)(i / XY), y = (int)((i - z * XY) / X), x = (int)(i - z * XY - y * X);
+            real lap[3];
+            lap_u_(&d, phi, x, y, z, lap);
+            g[i] = (r * dWa) + (lambda * lap[0]);
+            g[N + i] = (r * dWb) + (lambda * lap[1]);
+            g[2 * N + i] = (r * dWc) + (lambda * lap[2]);
+            if (W_out) W_out[i] = W;
+            ez += (double)r * (double)r;
+        }
+        part[zz] = ez;
     }
+    double e = 0.0;
+    for (int zz = 0; zz < d.Z; ++zz) e += part[zz];
+    free(part);
     return 0.5 * e;
 }
 
@@ -772,21 +781,36 @@ void FN(sob_pass_b)(const int *dims, const real *m, real *phi, real *max_norm, i
     const int64_t N = nvox(&d), X = d.X, XY = (int64_t)d.X * d.Y;
     real best = R(0);
     int64_t best_i = 0;
-    for (int64_t i = 0; i < N; ++i) {
-        fro_scell s;
-        sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
-        const int64_t b = s.base;
-        real u[3];
-        for (int c = 0; c < 3; ++c) {
-            const real *F = m + c * N;
-            u[c] = lerp_(lerp_(lerp_(F[b + 1 + X + XY], F[b + 1 + X], s.c), lerp_(F[b + 1 + XY], F[b + 1], s.c), s.b),
-                         lerp_(lerp_(F[b + X + XY], F[b + X], s.c), lerp_(F[b + XY], F[b], s.c), s.b), s.a);
+    /* per-thread first maximum (the gather reads m, never phi), merged so that ties go to
+     * the lowest index: the result of the serial loop with its strict '>' */
+#pragma omp parallel
+    {
+        real lbest = R(0);
+        int64_t lbest_i = INT64_MAX;
+#pragma omp for schedule(static)
+        for (int64_t i = 0; i < N; ++i) {
+            fro_scell s;
+            sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
+            const int64_t b = s.base;
+            real u[3];
+            for (int c = 0; c < 3; ++c) {
+                const real *F = m + c * N;
+                u[c] = lerp_(lerp_(lerp_(F[b + 1 + X + XY], F[b + 1 + X], s.c), lerp_(F[b + 1 + XY], F[b + 1], s.c), s.b),
+                             lerp_(lerp_(F[b + X + XY], F[b + X], s.c), lerp_(F[b + XY], F[b], s.c), s.b), s.a);
+            }
+            for (int c = 0; c < 3; ++c) phi[c * N + i] = phi[c * N + i] + u[c];
+            real nrm = sqrt_rd_((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
+            if (nrm > lbest) {
+                lbest = nrm;
+                lbest_i = i;
+            }
         }
-        for (int c = 0; c < 3; ++c) phi[c * N + i] = phi[c * N + i] + u[c];
-        real nrm = sqrt_rd_((u[0] * u[0] + u[1] * u[1]) + u[2] * u[2]);
-        if (nrm > best) {
-            best = nrm;
-            best_i = i;
+#pragma omp critical
+        {
+            if (lbest > best || (lbest == best && lbest_i < best_i && lbest > R(0))) {
+                best = lbest;
+                best_i = lbest_i;
+            }
         }
     }
     *max_norm = best;

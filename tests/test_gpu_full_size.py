@@ -1,0 +1,79 @@
+"""Parity at the size the throughput is quoted on.
+
+The 182x218x182 pair (N = 7,221,032) with the reference's params.ini values runs through
+the C ABI with the autotuned tile shapes of that size -- the launches of the timed
+200-iteration registration -- for a bounded number of iterations, and every field, both
+warped images and label maps, the max-update trace and the statistics are compared with
+the CPU oracle (fr_oracle.c, OpenMP) bit for bit.  The oracle takes about half a second
+per iteration at this size on 16 cores, so the iteration counts stay small; what an
+iteration computes does not depend on how many follow it.
+"""
+import numpy as np
+import pytest
+
+from fastreg_gb300 import FastReg, Params, _native as N, synthetic as sy
+from oracle import oracle as O
+from tests.helpers import assert_bitexact, rel_err
+
+pytestmark = pytest.mark.gpu
+
+DIMS = sy.CFG2.dims
+
+
+@pytest.fixture(scope="module")
+def pair(cuda):
+    d = sy.make_pair_torch(sy.CFG2, cuda)
+    return {k: v.cpu().numpy() for k, v in d.items()}
+
+
+def _to(dev, a):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+
+
+def test_reference_solver_at_full_size(cuda, pair):
+    d = pair
+    P = Params(volume_dims=DIMS, no_labels=8, max_iter=30, alpha=0.004, tau=0.2, w_reg=0.2, rho_0=1.0, p=2.0,
+               C=0.25, reset_iter=-1, max_update_norm=-1e-10)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    assert fr(iT, lT, iS, lS)
+    st = fr.stats()
+    norms, vox = fr.trace()
+    o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    assert st.iterations == o["iterations"] == 30
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi"], "psi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy(), o["psi_inv"], "psi_inv")
+    assert_bitexact(fr.get_field(N.FR_FIELD_V).cpu().numpy(), o["v"], "v")
+    assert_bitexact(fr.get_field(N.FR_FIELD_RHO).cpu().numpy(), o["rho"], "rho")
+    assert_bitexact(iT.cpu().numpy(), o["out_T"], "T o psi_inv")
+    assert_bitexact(iS.cpu().numpy(), o["out_S"], "S o psi")
+    assert_bitexact(lT.cpu().numpy(), o["out_labT"], "labels T o psi_inv")
+    assert_bitexact(lS.cpu().numpy(), o["out_labS"], "labels S o psi")
+    assert_bitexact(norms, o["trace_norm"], "max update norms")
+    assert_bitexact(vox, o["trace_idx"], "max update voxels")
+    os_ = O.stats(d["T"], d["labT"], o["out_S"], o["out_labS"], o["psi"], P.no_labels)
+    assert rel_err(st.e_data, os_["e_data"]) < 1e-12
+    assert rel_err(st.e_reg, os_["e_reg"]) < 1e-12
+    assert st.folds == os_["folds"]
+    assert st.dice_inter == list(os_["dice_inter"][:P.no_labels])
+    assert st.dice_count == list(os_["dice_count"][:P.no_labels])
+    fr.close()
+
+
+def test_sobolev_solver_at_full_size(cuda, pair):
+    d = pair
+    P = Params(volume_dims=DIMS, no_labels=8, max_iter=15, solver="sobolev", smooth_sigma=1.5, smooth_width=7,
+               damping=0.9, step=0.5)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    norms, vox = fr.trace()
+    o = O.sob_register(P, d["T"], d["S"])
+    assert o["iterations"] == 15
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["phi"], "phi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_V).cpu().numpy(), o["m"], "momentum")
+    assert_bitexact(norms, o["trace_norm"], "update norms")
+    assert_bitexact(vox, o["trace_idx"], "update voxels")
+    assert_bitexact(iS.cpu().numpy(), O.warp(o["phi"], d["S"]), "S o phi")
+    fr.close()
