@@ -48,9 +48,10 @@ struct TileSet {
 // defaults (AUTOTUNE=0), the autotuner's usual choice on the 182x218x182 pair: slices per
 // tile, and whether each tile is its own block (scheduled by the hardware) instead of a
 // persistent grid at the occupancy limit
-static const int kDefaultDepth[R_COUNT] = {4, 24, 24, 16, 32, 8};
-static const bool kDefaultPerTile[R_COUNT] = {false, true, false, false, true, false};
+static const int kDefaultDepth[R_COUNT] = {16, 24, 24, 12, 32, 8};
+static const bool kDefaultPerTile[R_COUNT] = {true, true, false, true, true, false};
 static const int kMinDepth = 1;  // thin tiles give small volumes enough blocks
+static const int kTuneWarmIters = 20;  // iterations run before the autotuner times shapes
 
 struct fr_handle {
     fr_params P;
@@ -229,7 +230,14 @@ const void* role_fn(const fr_handle* h, int r) {
     }
 }
 
-size_t role_smem(int r) { return r == R_PA ? frg::ref_pass_a_smem_bytes() : 0; }
+size_t role_smem(int r) {
+    switch (r) {
+        case R_LAP: return frg::ref_laplacian_smem_bytes();
+        case R_PA: return frg::ref_pass_a_smem_bytes();
+        case R_SG: return frg::sob_grad_smem_bytes();
+        default: return 0;
+    }
+}
 
 typedef std::array<Shape, R_COUNT> Shapes;
 
@@ -446,7 +454,7 @@ frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
 int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev) {
     frg::RefIterArgs a = ref_args(h, iter, t);
     if (ev) cudaEventRecord(ev[0], s);
-    frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, 0, s>>>(a);
+    frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, frg::ref_laplacian_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
@@ -675,15 +683,18 @@ std::string size_class(const fr_handle* h) {
 std::mutex g_tune_mu;
 std::map<std::string, Shapes> g_tuned;
 
-int launch_role(fr_handle* h, int r, float t, cudaStream_t s) {
+int launch_role(fr_handle* h, int r, int iter, float t, cudaStream_t s) {
     frg::RefIterArgs ra{};
     frg::SobIterArgs sa{};
     void* args[1];
+    // no pair converges while shapes are timed (a stopped pair's tiles would be skipped)
     if (r == R_LAP || r == R_PA || r == R_PB) {
-        ra = ref_args(h, 1, t);
+        ra = ref_args(h, iter, t);
+        ra.max_update_norm = -INFINITY;
         args[0] = &ra;
     } else {
-        sa = sob_args(h, 1);
+        sa = sob_args(h, iter);
+        sa.max_update_norm = -INFINITY;
         args[0] = &sa;
     }
     FR_CUDA(h, cudaLaunchKernel(role_fn(h, r), dim3(h->ts[r].grid), dim3(256), args, role_smem(r), s));
@@ -701,13 +712,24 @@ int autotune(fr_handle* h, cudaStream_t s) {
             return rc;
         }
     }
-    // a state to time on: the packed cohort of the current registration
+    // a state to time on: the packed cohort of the current registration after a few
+    // iterations (an even number, so that the double-buffered fields are back in buffer
+    // 0), where the velocity or momentum that the update kernels gather is no longer zero
+    // and the gathers leave the grid points; shapes timed at the identity state chose a
+    // sobolev update 7% slower than the best
     FR_CUDA(h, cudaMemsetAsync(h->stop, 0, sizeof(int) * h->npairs, s));
     frg::IoArgs io = io_args(h);
     io.keep_state = 0;
     frg::pack_init_kernel<<<h->grid_io, 256, 0, s>>>(io);
     FR_LAUNCHED(h);
-    const float t = h->P.alpha;  // the first iteration's t
+    const std::vector<float> ts = t_schedule(h->P);
+    const int warm = std::min(kTuneWarmIters, (h->trace_cap - 1) / 2 * 2);  // the trace holds iteration warm + 1
+    for (int it = 1; it <= warm; ++it) {
+        int rc = launch_iter(h, it, ts[it - 1], s);
+        if (rc != FR_OK) return rc;
+    }
+    const int iter = warm + 1;
+    const float t = iter <= (int)ts.size() ? ts[iter - 1] : h->P.alpha;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     FR_CUDA(h, cudaEventCreate(&e0));
     FR_CUDA(h, cudaEventCreate(&e1));
@@ -732,9 +754,9 @@ int autotune(fr_handle* h, cudaStream_t s) {
                     rc = fail(h, FR_ERR_CUDA, "autotune: memset failed");
                     break;
                 }
-                rc = launch_role(h, r, t, s);  // warm-up
+                rc = launch_role(h, r, iter, t, s);  // warm-up
                 if (rc == FR_OK) cudaEventRecord(e0, s);
-                for (int k = 0; k < 3 && rc == FR_OK; ++k) rc = launch_role(h, r, t, s);
+                for (int k = 0; k < 3 && rc == FR_OK; ++k) rc = launch_role(h, r, iter, t, s);
                 if (rc != FR_OK) break;
                 cudaEventRecord(e1, s);
                 if (cudaEventSynchronize(e1) != cudaSuccess) {

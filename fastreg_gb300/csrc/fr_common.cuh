@@ -220,6 +220,25 @@ __device__ __forceinline__ void cp_async_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(Pending) : "memory");
 }
 
+// ---- slices of a 32 x 8 column tile staged in shared memory ----
+// A staged slice of a plane with y halo H is 8 + 2H rows (y0 - H .. y0 + 7 + H) of
+// kStageChunks aligned 16-byte chunks (columns x0 - 4 .. x0 + 35; column x0 + tx sits at
+// row offset tx + kStageXO).  Thread e copies chunk e of every slice and component of the
+// tile: its shared-memory offset is 4e floats, and its offset inside a slice, fixed for
+// the tile, is returned here (-1: no chunk, or the chunk lies outside the padded volume,
+// where no voxel of the tile reads).
+constexpr int kStageXO = 4, kStageW = kTileX + 2 * kStageXO, kStageChunks = kStageW / 4;
+template <int H>
+__device__ __forceinline__ int stage_offset(int e, int Y, int Xp, int x0, int y0) {
+    constexpr int R = kTileY + 2 * H;
+    static_assert(R * kStageChunks <= 256, "one chunk per thread of a 256-thread block");
+    if (e >= R * kStageChunks) return -1;
+    const int r = e / kStageChunks, k = e - r * kStageChunks;
+    const int y = y0 - H + r, x = x0 - kStageXO + 4 * k;
+    if (y < 0 || y >= Y || x < 0 || x >= Xp) return -1;
+    return Xp * y + x;
+}
+
 // sqrt rounded toward -inf (reference norm(), include/cuda/cuda_utils.hpp:251-253)
 __device__ __forceinline__ float norm3_rd(float x, float y, float z) {
     return __fsqrt_rd((x * x + y * y) + z * z);

@@ -43,6 +43,7 @@ struct RefIterArgs {
     unsigned int* counter;     // last-block ticket of pass B
 };
 
+size_t ref_laplacian_smem_bytes();  // dynamic shared memory of ref_laplacian_kernel
 __global__ void ref_laplacian_kernel(RefIterArgs a);
 size_t ref_pass_a_smem_bytes();  // dynamic shared memory of ref_pass_a_kernel
 __global__ void ref_pass_a_kernel(RefIterArgs a);

@@ -49,34 +49,88 @@ __device__ __forceinline__ SobCell sob_locate(const Pair& P, float px, float py,
     return s;
 }
 
+// W = S o phi, r = W - T, the exact trilinear gradient of the interpolant, the graph
+// Laplacian of u = phi - x and the FP64 data energy.  A block owns a 32 x 8 column tile
+// and marches z: phi's three components (tile rows plus a 1-voxel halo) and T are staged
+// slice by slice into a shared-memory ring by 16-byte cp.async kGAhead slices ahead of the
+// compute; the eight corners of S are gathered through L1.
+namespace {
+constexpr int kGAhead = 2;        // slices in flight ahead of the one computed
+constexpr int kGS = 3 + kGAhead;  // ring slots: slices z - 1, z, z + 1 and those in flight
+constexpr int kGW = kStageW, kGPlane = kGW * (kTileY + 2), kGTPlane = kTileX * kTileY;
+}  // namespace
+
+size_t sob_grad_smem_bytes() { return sizeof(float) * kGS * (3 * kGPlane + kGTPlane); }
+
 __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
+    extern __shared__ __align__(16) float ring[];  // phi [3][kGS][10][kGW], then T [kGS][8][32]
+    float* tring = ring + 3 * kGS * kGPlane;
     __shared__ double red[32];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     for (int t = blockIdx.x; t < a.ntiles_g; t += gridDim.x) {
         const Tile tl = a.tiles_g[t];
         if (a.stop[tl.x]) continue;  // uniform over the block
         const Pair P = a.pairs[tl.x];
-        const int x = tl.y + (int)(threadIdx.x & 31), y = tl.z + (int)(threadIdx.x >> 5);
+        const int Y = P.Y, Z = P.Z, Xp = P.Xp, XYp = P.Xp * P.Y;  // strides of the packed arrays
+        const long long NT = a.NT;
+        const float* __restrict__ S = a.S + P.off;
+        const float* __restrict__ Tg = a.T + P.off;
+        const float* __restrict__ Fg[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
+        float* G[3] = {a.g + P.off, a.g + NT + P.off, a.g + 2 * NT + P.off};
+        const int x = tl.y + tx, y = tl.z + ty;
+        const bool inside = x < P.X && y < Y;
+        const int z0 = tl.w, z1 = min(tl.w + a.depth_g, Z);
+        const int gq = stage_offset<1>(threadIdx.x, Y, Xp, tl.y, tl.z);
+        // T: thread e < 64 copies chunk e & 7 of tile row e >> 3 (x0 is a multiple of 32)
+        const int tr = (int)threadIdx.x >> 3, tk = (int)threadIdx.x & 7;
+        const int gt = (threadIdx.x < 64 && tl.z + tr < Y && tl.y + 4 * tk < Xp) ? Xp * (tl.z + tr) + tl.y + 4 * tk
+                                                                                 : -1;
+        auto stage = [&](int zs, int sl) {  // slice zs of phi (and T) into slot sl
+            if (zs < 0 || zs >= Z) return;
+            if (gq >= 0) {
+                float* dst = ring + sl * kGPlane + 4 * threadIdx.x;
+                const int off = gq + XYp * zs;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) cp_async16(dst + c * kGS * kGPlane, Fg[c] + off);
+            }
+            if (gt >= 0) cp_async16(tring + sl * kGTPlane + 4 * threadIdx.x, Tg + gt + XYp * zs);
+        };
         double e = 0.0;
-        if (x < P.X && y < P.Y) {
-            const long long NT = a.NT;
-            const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
-            const float* __restrict__ S = a.S + P.off;
-            const float* __restrict__ T = a.T + P.off;
-            const float* __restrict__ phi0 = a.phi + P.off;
-            const float* __restrict__ phi1 = phi0 + NT;
-            const float* __restrict__ phi2 = phi1 + NT;
-            float* g0 = a.g + P.off;
-            float* g1 = g0 + NT;
-            float* g2 = g1 + NT;
-            const int z1 = min(tl.w + a.depth_g, P.Z);
-            for (int z = tl.w; z < z1; ++z) {
-                const int i = x + X * y + XY * z;
-                const SobCell s = sob_locate(P, __ldg(phi0 + i), __ldg(phi1 + i), __ldg(phi2 + i));
+        __syncthreads();  // the previous tile is done with the ring
+        // prologue: slices z0 - 1 .. z0 + 1 (one group), then one group per slice ahead
+        stage(z0 - 1, 0);
+        stage(z0, 1);
+        stage(z0 + 1, 2);
+        cp_async_commit();
+#pragma unroll
+        for (int k = 1; k < kGAhead; ++k) {
+            if (z0 + 1 + k <= z1) stage(z0 + 1 + k, 2 + k);
+            cp_async_commit();
+        }
+        int sm = 0;  // slot of slice z - 1 (z, z + 1 follow it in the ring)
+        const int c0 = (ty + 1) * kGW + tx + kStageXO;
+        for (int z = z0; z < z1; ++z) {
+            cp_async_wait<kGAhead - 1>();  // slice z + 1 has landed ...
+            __syncthreads();               // ... for every thread, and slice z - 2's slot is free
+            {
+                int sl = sm + 2 + kGAhead;  // the slot of slice z - 2
+                sl = sl >= kGS ? sl - kGS : sl;
+                if (z + 1 + kGAhead <= z1) stage(z + 1 + kGAhead, sl);  // reads reach z1
+                cp_async_commit();
+            }
+            const int s0 = sm + 1 >= kGS ? sm + 1 - kGS : sm + 1;
+            const int sp = s0 + 1 >= kGS ? s0 + 1 - kGS : s0 + 1;
+            if (inside) {
+                const int i = x + Xp * y + XYp * z;
+                const float* q[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) q[c] = ring + (c * kGS + s0) * kGPlane + c0;
+                const SobCell s = sob_locate(P, q[0][0], q[1][0], q[2][0]);
                 const int b = (int)s.base;
                 const float f000 = __ldg(S + b), f100 = __ldg(S + b + 1);
-                const float f010 = __ldg(S + b + X), f110 = __ldg(S + b + 1 + X);
-                const float f001 = __ldg(S + b + XY), f101 = __ldg(S + b + 1 + XY);
-                const float f011 = __ldg(S + b + X + XY), f111 = __ldg(S + b + 1 + X + XY);
+                const float f010 = __ldg(S + b + Xp), f110 = __ldg(S + b + 1 + Xp);
+                const float f001 = __ldg(S + b + XYp), f101 = __ldg(S + b + 1 + XYp);
+                const float f011 = __ldg(S + b + Xp + XYp), f111 = __ldg(S + b + 1 + Xp + XYp);
                 const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
                 const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
                 const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
@@ -86,30 +140,34 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                 const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
                                                   lerpf_(f011 - f010, f001 - f000, s.b), s.a)
                                          : 0.f;
-                const float r = W - __ldg(T + i);
+                const float r = W - tring[s0 * kGTPlane + ty * kTileX + tx];
                 // graph Laplacian of u = phi - x, neighbours inside the grid, order -x,+x,-y,+y,-z,+z
-                const bool ok[6] = {x > 0, x < P.X - 1, y > 0, y < P.Y - 1, z > 0, z < P.Z - 1};
-                const int off[6] = {-1, 1, -X, X, -XY, XY};
+                const bool ok[6] = {x > 0, x < P.X - 1, y > 0, y < Y - 1, z > 0, z < Z - 1};
                 float lap[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    const float* __restrict__ Pc = c == 0 ? phi0 : (c == 1 ? phi1 : phi2);
-                    const float pc = __ldg(Pc + i);
+                    const float* qc = q[c];
+                    const float* qm = ring + (c * kGS + sm) * kGPlane + c0;
+                    const float* qp = ring + (c * kGS + sp) * kGPlane + c0;
+                    const float pc = qc[0];
+                    const float nb[6] = {qc[-1], qc[1], qc[-kGW], qc[kGW], qm[0], qp[0]};
                     float acc = 0.f;
 #pragma unroll
                     for (int k = 0; k < 6; ++k) {
                         if (!ok[k]) continue;
                         const float delta = (k / 2 == c) ? ((k & 1) ? 1.f : -1.f) : 0.f;
-                        acc = acc + ((pc - __ldg(Pc + i + off[k])) + delta);
+                        acc = acc + ((pc - nb[k]) + delta);
                     }
                     lap[c] = acc;
                 }
-                g0[i] = (r * dWa) + (P.w_reg * lap[0]);
-                g1[i] = (r * dWb) + (P.w_reg * lap[1]);
-                g2[i] = (r * dWc) + (P.w_reg * lap[2]);
+                G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
+                G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
+                G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
                 e += (double)r * (double)r;
             }
+            sm = s0;
         }
+        cp_async_wait<0>();
         e = block_sum_f64(e, red);
         if (threadIdx.x == 0) atomicAdd(a.energy + (long long)(a.iter - 1) * a.npairs + tl.x, 0.5 * e);
     }
@@ -336,7 +394,7 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
 
 cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t s, cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
-    sob_grad_kernel<<<grids[0], 256, 0, s>>>(a);
+    sob_grad_kernel<<<grids[0], 256, sob_grad_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     switch (a.radius) {
         case 0: sob_smooth3_kernel<0><<<grids[1], 256, 0, s>>>(a); break;

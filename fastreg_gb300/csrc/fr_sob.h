@@ -57,6 +57,7 @@ struct SobIterArgs {
 // and rounded to float.
 void gaussian_taps(float sigma, int width, float* taps);
 
+size_t sob_grad_smem_bytes();  // dynamic shared memory of sob_grad_kernel
 __global__ void sob_grad_kernel(SobIterArgs a);
 const void* sob_smooth3_fn(int radius);  // the smoothing kernel instance for a radius
 __global__ void sob_pass_b_kernel(SobIterArgs a);

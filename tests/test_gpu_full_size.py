@@ -53,8 +53,9 @@ def test_reference_solver_at_full_size(cuda, pair):
     assert_bitexact(norms, o["trace_norm"], "max update norms")
     assert_bitexact(vox, o["trace_idx"], "max update voxels")
     os_ = O.stats(d["T"], d["labT"], o["out_S"], o["out_labS"], o["psi"], P.no_labels)
-    assert rel_err(st.e_data, os_["e_data"]) < 1e-12
-    assert rel_err(st.e_reg, os_["e_reg"]) < 1e-12
+    # FP64 sums of 7.2 M terms added in another order (per-tile partials on the GPU)
+    assert rel_err(st.e_data, os_["e_data"]) < 1e-10
+    assert rel_err(st.e_reg, os_["e_reg"]) < 1e-10
     assert st.folds == os_["folds"]
     assert st.dice_inter == list(os_["dice_inter"][:P.no_labels])
     assert st.dice_count == list(os_["dice_count"][:P.no_labels])
