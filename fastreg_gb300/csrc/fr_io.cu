@@ -238,34 +238,59 @@ __global__ void __launch_bounds__(256) warp_kernel(const float* __restrict__ pos
 }
 
 // Four consecutive voxels per thread (32-bit indices): 16-byte loads of the three
-// position planes, 32 independent corner loads in flight, a 16-byte store of the
-// intensities and an 8-byte store of the labels.  The caller guarantees N = X*Y*Z a
-// multiple of 4 below 2^31 and 16-byte (pos, out) / 8-byte (out_lab) aligned buffers;
-// per voxel the arithmetic is warp_kernel's.
+// position planes, issued one grid-stride item ahead so that they are in flight with the
+// current item's 32 corner and 4 label loads; a 16-byte store of the intensities and an
+// 8-byte store of the labels.  The caller guarantees N = X*Y*Z a multiple of 4 below 2^31
+// and 16-byte (pos, out) / 8-byte (out_lab) aligned buffers; per voxel the arithmetic is
+// warp_kernel's (corners past the last voxel, of weight 0, clamped as tri_unchecked32
+// does).
 __global__ void __launch_bounds__(256) warp4_kernel(const float* __restrict__ pos, const float* __restrict__ img,
                                                     const int16_t* __restrict__ lab, float* __restrict__ out,
                                                     int16_t* __restrict__ out_lab, int X, int Y, int Z) {
-    const int N = X * Y * Z, N4 = N >> 2, XY = X * Y;
+    const int N = X * Y * Z, N4 = N >> 2, XY = X * Y, last = N - 1;
     const float4* __restrict__ p4 = reinterpret_cast<const float4*>(pos);
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < N4; t += gridDim.x * blockDim.x) {
-        const float4 px = __ldg(p4 + t), py = __ldg(p4 + N4 + t), pz = __ldg(p4 + 2 * N4 + t);
+    const int stride = gridDim.x * blockDim.x;
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    float4 npx = make_float4(0.f, 0.f, 0.f, 0.f), npy = npx, npz = npx;
+    if (t < N4) {
+        npx = __ldg(p4 + t);
+        npy = __ldg(p4 + N4 + t);
+        npz = __ldg(p4 + 2 * N4 + t);
+    }
+    for (; t < N4; t += stride) {
+        const float4 px = npx, py = npy, pz = npz;
+        if (t + stride < N4) {  // the next item's positions load while this one's corners do
+            npx = __ldg(p4 + t + stride);
+            npy = __ldg(p4 + N4 + t + stride);
+            npz = __ldg(p4 + 2 * N4 + t + stride);
+        }
         const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w},
                     zs[4] = {pz.x, pz.y, pz.z, pz.w};
-        float r[4];
-        int b[4];
+        Cell32 cl[4];
+        float f[4][8];
+        short lb[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            const Cell32 cl = locate32(X, Y, Z, X, xs[k], ys[k], zs[k]);
-            r[k] = tri_unchecked32(img, X, XY, N, cl);
-            b[k] = cl.base;
+            cl[k] = locate32(X, Y, Z, X, xs[k], ys[k], zs[k]);
+            const int b = cl[k].base;
+            const int o[8] = {min(b + 1 + X + XY, last), min(b + 1 + X, last), min(b + 1 + XY, last), min(b + 1, last),
+                              min(b + X + XY, last),     min(b + X, last),     min(b + XY, last),     b};
+#pragma unroll
+            for (int j = 0; j < 8; ++j) f[k][j] = __ldg(img + o[j]);
+            if (out_lab) lb[k] = __ldg(lab + b);
         }
+        float r[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            r[k] = trilerp(f[k][0], f[k][1], f[k][2], f[k][3], f[k][4], f[k][5], f[k][6], f[k][7], cl[k].a, cl[k].b,
+                           cl[k].c);
         reinterpret_cast<float4*>(out)[t] = make_float4(r[0], r[1], r[2], r[3]);
         if (out_lab) {
             short4 l;
-            l.x = __ldg(lab + b[0]);
-            l.y = __ldg(lab + b[1]);
-            l.z = __ldg(lab + b[2]);
-            l.w = __ldg(lab + b[3]);
+            l.x = lb[0];
+            l.y = lb[1];
+            l.z = lb[2];
+            l.w = lb[3];
             reinterpret_cast<short4*>(out_lab)[t] = l;
         }
     }
