@@ -464,8 +464,8 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
     return FR_OK;
 }
 
-// kernels launched per iteration
-int kernels_per_iter(const fr_handle* h) { return 3; }
+// kernels launched per iteration (three in either solver)
+int kernels_per_iter(const fr_handle*) { return 3; }
 
 frg::SobIterArgs sob_args(fr_handle* h, int iter) {
     frg::SobIterArgs a{};
@@ -731,8 +731,10 @@ int autotune(fr_handle* h, cudaStream_t s) {
     const int iter = warm + 1;
     const float t = iter <= (int)ts.size() ? ts[iter - 1] : h->P.alpha;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    FR_CUDA(h, cudaEventCreate(&e0));
-    FR_CUDA(h, cudaEventCreate(&e1));
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return fail(h, FR_ERR_CUDA, "autotune: cudaEventCreate failed");
+    }
     Shapes best = default_shapes(h);
     int rc = FR_OK;
     for (int r : active_roles(h)) {
@@ -1273,26 +1275,29 @@ int fr_time_kernels(fr_handle* h, int iters, float* ms, int* n_kernels, void* st
     if (!h->have_state) return fail(h, FR_ERR_STATE, "fr_time_kernels before fr_begin");
     cudaStream_t s = (cudaStream_t)stream;
     const int nk = kernels_per_iter(h);
-    cudaEvent_t ev[6];
-    for (int k = 0; k <= nk; ++k) FR_CUDA(h, cudaEventCreate(&ev[k]));
+    cudaEvent_t ev[6] = {};
+    int rc = FR_OK;
+    for (int k = 0; k <= nk && rc == FR_OK; ++k)
+        if (cudaEventCreate(&ev[k]) != cudaSuccess) rc = fail(h, FR_ERR_CUDA, "fr_time_kernels: cudaEventCreate failed");
     std::vector<double> acc(nk, 0.0);
     std::vector<float> ts = t_schedule(h->P);
-    int rc = FR_OK;
     for (int it = 1; it <= iters && rc == FR_OK; ++it) {
         // iterations cycle through the schedule; every kernel reads what it would read
         const int slot = 1 + (it - 1) % std::max(h->trace_cap, 1);
         const float t = ts.empty() ? h->P.alpha : ts[(slot - 1) % ts.size()];
         rc = launch_iter(h, slot, t, s, ev);
         if (rc != FR_OK) break;
-        FR_CUDA(h, cudaEventSynchronize(ev[nk]));
-        for (int k = 0; k < nk; ++k) {
+        cudaError_t e = cudaEventSynchronize(ev[nk]);
+        for (int k = 0; k < nk && e == cudaSuccess; ++k) {
             float m = 0.f;
-            FR_CUDA(h, cudaEventElapsedTime(&m, ev[k], ev[k + 1]));
+            e = cudaEventElapsedTime(&m, ev[k], ev[k + 1]);
             acc[k] += m;
         }
+        if (e != cudaSuccess) rc = fail(h, FR_ERR_CUDA, "fr_time_kernels: %s", cudaGetErrorString(e));
         h->last_iter = slot;
     }
-    for (int k = 0; k <= nk; ++k) cudaEventDestroy(ev[k]);
+    for (int k = 0; k <= nk; ++k)
+        if (ev[k]) cudaEventDestroy(ev[k]);
     if (rc != FR_OK) return rc;
     for (int k = 0; k < nk; ++k) ms[k] = (float)(acc[k] / iters);
     if (n_kernels) *n_kernels = nk;
