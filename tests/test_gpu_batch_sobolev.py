@@ -18,7 +18,7 @@ def _to(dev, a):
 def test_batch_equals_pairs_alone(cuda, solver):
     """A cohort of uneven pairs in one set of launches gives, pair by pair, the bits
     of each pair registered alone (and of the oracle)."""
-    dims_list = [(20, 18, 16), (33, 17, 21), (16, 24, 12), (40, 9, 10)]
+    dims_list = [(20, 18, 16), (33, 17, 21), (16, 24, 12), (40, 9, 10), (4, 4, 5)]
     kw = dict(no_labels=4, max_iter=25, alpha=0.02, solver=solver, step=0.5, damping=0.9)
     pairs_np = [images(d, 50 + k) for k, d in enumerate(dims_list)]
     P = Params(volume_dims=dims_list[0], **kw)
@@ -45,7 +45,7 @@ def test_batch_equals_pairs_alone(cuda, solver):
         assert st.iterations == 25
 
 
-@pytest.mark.parametrize("dims", [(12, 10, 9), (33, 17, 20)])
+@pytest.mark.parametrize("dims", [(4, 5, 4), (12, 10, 9), (33, 17, 20)])
 def test_sobolev_registration(cuda, dims):
     d = images(dims, 11 + dims[0])
     P = Params(volume_dims=dims, no_labels=4, max_iter=30, solver="sobolev", smooth_sigma=1.5, smooth_width=7,

@@ -22,7 +22,7 @@ def _params(dims, **kw):
     return Params(**base)
 
 
-@pytest.mark.parametrize("dims", [(7, 9, 11), (33, 17, 20), (40, 36, 30)])
+@pytest.mark.parametrize("dims", [(4, 4, 4), (5, 6, 4), (7, 9, 11), (33, 17, 20), (40, 36, 30)])
 @pytest.mark.parametrize("iter_no", [1, 2, 7])
 def test_one_iteration_from_random_state(cuda, dims, iter_no):
     """One iteration (L, pass A, pass B) from a random mid-registration state."""
@@ -59,7 +59,7 @@ def test_one_iteration_from_random_state(cuda, dims, iter_no):
     fr.close()
 
 
-@pytest.mark.parametrize("dims,iters", [((12, 10, 9), 30), ((24, 20, 18), 60), ((64, 64, 64), 200)])
+@pytest.mark.parametrize("dims,iters", [((4, 5, 4), 20), ((12, 10, 9), 30), ((24, 20, 18), 60), ((64, 64, 64), 200)])
 def test_full_registration(cuda, dims, iters):
     """A whole registration through FastReg::operator() semantics (in place)."""
     import torch
