@@ -61,12 +61,12 @@ def load_peaks():
 
 def load_traffic(kernel: str):
     """dram bytes per launch of `kernel` at the bench workload, from the committed ncu
-    summary (a line 'dram_bytes_per_launch_cfg2: <int>'), or None."""
-    f = ROOT / "profiles" / f"{kernel}_cfg2.txt"
+    summary (a line 'dram_bytes_per_launch: <int>'), or None."""
+    f = ROOT / "profiles" / f"{kernel}_182x218x182.txt"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch_cfg2:"):
+        if line.startswith("dram_bytes_per_launch:"):
             try:
                 return int(float(line.split(":", 1)[1].strip()))
             except ValueError:
@@ -171,7 +171,7 @@ def run_reference_arm(args):
     obuild.build()
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    data = sy.make_pair(sy.CFG2)
+    data = sy.make_pair(sy.PAIR_182X218X182)
     P = reference_params()
     vals = []
     for step in range(args.warmup + args.steps):
@@ -183,7 +183,7 @@ def run_reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "cfg2: one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
+        "config": {"workload": "one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
                    "solver": "reference", "sample": "1 and 2 iterations of the full volume per step, extrapolated "
                                                    "to 200 iterations"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
@@ -228,7 +228,7 @@ def profile_case(args):
         return 0
     from fastreg_gb300 import FastReg, synthetic as sy, warp, _native as N
     dev = torch.device("cuda", 0)
-    data = sy.make_pair(sy.CFG2)
+    data = sy.make_pair(sy.PAIR_182X218X182)
     P = reference_params(DIMS, args.iters, solver=args.solver)
     fr = FastReg(P)
     fresh = lambda: [torch.from_numpy(data[k]).to(dev) for k in ("T", "labT", "S", "labS")]  # noqa: E731
@@ -281,12 +281,12 @@ def small_pair_timing(dev, stream, reps=5):
     solvers, inputs resident; after warm-up registrations (which also tune the shapes)."""
     import torch
     from fastreg_gb300 import FastReg, synthetic as sy
-    d = sy.make_pair_torch(sy.CFG1, dev)
+    d = sy.make_pair_torch(sy.PAIR_64CUBE, dev)
     pristine = [d[k] for k in ("T", "labT", "S", "labS")]
     work = [t.clone() for t in pristine]
-    out = {"dims": list(sy.CFG1.dims), "iterations": ITERS}
+    out = {"dims": list(sy.PAIR_64CUBE.dims), "iterations": ITERS}
     for solver in ("reference", "sobolev"):
-        fr = FastReg(reference_params(dims=sy.CFG1.dims, solver=solver))
+        fr = FastReg(reference_params(dims=sy.PAIR_64CUBE.dims, solver=solver))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
             for rep in range(3 + reps):
@@ -471,7 +471,7 @@ def main():
     from fastreg_gb300 import FastReg, synthetic as sy, warp, _native as N
     import ctypes as C
 
-    spec = sy.CFG2
+    spec = sy.PAIR_182X218X182
     if ws > 1:
         spec = sy.PairSpec(**{**spec.__dict__, "seed": spec.seed + rank})
     data = sy.make_pair(spec)
@@ -561,7 +561,7 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded: 400 Gaussian blobs + N(0,0.01), smooth velocity sigma 6, max disp 6, 8 classes)",
-        "config": {"workload": "cfg2: one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
+        "config": {"workload": "one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
                    "solver": "reference", "voxels": int(np.prod(DIMS)), "iterations": ITERS,
                    "other_solver": "the workload's Gaussian-smoothed (sobolev) settings -- width 7, sigma 1.5, "
                                    "damping 0.9, step 0.5 -- are timed on the same pair in the 'sobolev' block",
@@ -651,7 +651,7 @@ def main():
         frs.close()
 
         # the 64^3 single-pair workload (the CPU-runnable configuration), both solvers
-        line["cfg1_64cube"] = small_pair_timing(dev, stream)
+        line["pair_64cube"] = small_pair_timing(dev, stream)
 
         # batched cohort against plain per-pair calls: 16 uneven pairs, 200 iterations each
         line["batched"] = batched_vs_plain(dev, stream)

@@ -29,9 +29,10 @@ class PairSpec:
     seed: int = 1000
 
 
-# the workloads of the benchmark configurations
-CFG1 = PairSpec(dims=(64, 64, 64), n_blobs=40, vel_sigma=4.0, max_disp=3.0, n_classes=4, seed=1000)
-CFG2 = PairSpec(dims=(182, 218, 182), n_blobs=400, noise=0.01, vel_sigma=6.0, max_disp=6.0, n_classes=8, seed=2000)
+# the single-pair workloads: a 64^3 pair (4 label classes, max displacement 3 voxels) and
+# the 182x218x182 pair the throughput is quoted on (8 classes, max displacement 6, noise)
+PAIR_64CUBE = PairSpec(dims=(64, 64, 64), n_blobs=40, vel_sigma=4.0, max_disp=3.0, n_classes=4, seed=1000)
+PAIR_182X218X182 = PairSpec(dims=(182, 218, 182), n_blobs=400, noise=0.01, vel_sigma=6.0, max_disp=6.0, n_classes=8, seed=2000)
 
 
 def blobs(dims, n, sigma_range, amp_range, rng) -> np.ndarray:

@@ -17,12 +17,12 @@ from tests.helpers import assert_bitexact, rel_err
 
 pytestmark = pytest.mark.gpu
 
-DIMS = sy.CFG2.dims
+DIMS = sy.PAIR_182X218X182.dims
 
 
 @pytest.fixture(scope="module")
 def pair(cuda):
-    d = sy.make_pair_torch(sy.CFG2, cuda)
+    d = sy.make_pair_torch(sy.PAIR_182X218X182, cuda)
     return {k: v.cpu().numpy() for k, v in d.items()}
 
 

@@ -28,8 +28,8 @@ def test_full_size_parity_and_speed_against_reference_kernels(cuda):
         # built from the reference sources where they are present; the committed golden
         # fixtures (test_cuda_path_matches_reference_kernels) pin the path without them
         pytest.skip("reference kernels (oracle/_ref/*.cubin) are not built here; oracle/ref_build.py builds them")
-    d = sy.make_pair(sy.CFG2)
-    dims = sy.CFG2.dims
+    d = sy.make_pair(sy.PAIR_182X218X182)
+    dims = sy.PAIR_182X218X182.dims
     P = Params(volume_dims=dims, no_labels=8, max_iter=200, alpha=0.004, tau=0.2, w_reg=0.2, rho_0=1.0, p=2.0,
                C=0.25, reset_iter=-1, max_update_norm=-1e-10)
     ref = ref_runner.register(P, d["T"], d["labT"], d["S"], d["labS"], timing=True)
