@@ -147,3 +147,52 @@ def test_per_pair_w_reg(cuda, solver):
                                                        pairs_np[0]["T"], pairs_np[0]["S"]))
     assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi" if solver == "reference" else "phi"], "W_REG")
     fr.close()
+
+
+@pytest.mark.parametrize("solver", ["reference", "sobolev"])
+def test_batched_convergence_and_keep_state(cuda, solver):
+    """One MAX_UPDATE_NORM for a cohort whose pairs converge at different iterations (the
+    graph keeps launching; a stopped pair's tiles are skipped): each pair stops where the
+    oracle's loop breaks, with the oracle's fields.  For the reference solver a second
+    call with KEEP_STATE=1 then continues every pair from its own final state, whatever
+    the parity of the iteration it stopped at."""
+    dims_list = [(24, 20, 18), (20, 18, 16), (16, 24, 12), (18, 15, 21)]
+    pairs_np = [images(d, 1300 + k) for k, d in enumerate(dims_list)]
+    kw = dict(no_labels=4, max_iter=40, alpha=0.02, solver=solver, step=0.5, damping=0.9)
+
+    def oracle(dims, p, P, state=None):
+        if solver == "reference":
+            return O.ref_register(P, p["T"], p["labT"], p["S"], p["labS"], state=state)
+        o = O.sob_register(P, p["T"], p["S"])
+        o["psi"] = o["phi"]
+        return o
+
+    # thresholds inside the pairs' update-norm traces: the reference solver's norms halve at
+    # iteration 2 and then grow (stops at 1, 2, 2 and none); the sobolev solver's rise and
+    # decay (stops at 40, 24, 1 and none)
+    kw["max_update_norm"] = 3e-6 if solver == "reference" else 2.7e-3
+    expect = [oracle(d, p, Params(volume_dims=d, **kw)) for d, p in zip(dims_list, pairs_np)]
+    stops = [o["iterations"] if o["converged"] else None for o in expect]
+    assert None in stops and len(set(stops)) >= 3, stops
+
+    fr = FastReg(Params(volume_dims=dims_list[0], keep_state=1 if solver == "reference" else 0, **kw))
+    bufs = [tuple(_to(cuda, p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+    fr.register_batch(bufs)
+    for k, o in enumerate(expect):
+        st = fr.stats(pair=k)
+        assert st.iterations == o["iterations"] and st.converged == o["converged"], (k, st.iterations, o["iterations"])
+        assert_bitexact(fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy(), o["psi"], f"pair {k} psi")
+        if solver == "reference":
+            assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV, pair=k).cpu().numpy(), o["psi_inv"], f"pair {k} psi_inv")
+            assert_bitexact(bufs[k][2].cpu().numpy(), o["out_S"], f"pair {k} S o psi")
+            assert_bitexact(bufs[k][0].cpu().numpy(), o["out_T"], f"pair {k} T o psi_inv")
+    if solver != "reference":
+        return
+    bufs = [tuple(_to(cuda, p[k]) for k in ("T", "labT", "S", "labS")) for p in pairs_np]
+    fr.register_batch(bufs)
+    for k, (d, p, o1) in enumerate(zip(dims_list, pairs_np, expect)):
+        state = dict(rho=o1["rho"], v=o1["v"], psi=o1["psi"], psi_inv=o1["psi_inv"])
+        o2 = oracle(d, p, Params(volume_dims=d, keep_state=1, **kw), state=state)
+        assert fr.stats(pair=k).iterations == o2["iterations"]
+        assert_bitexact(fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy(), o2["psi"], f"pair {k} psi, 2nd call")
+        assert_bitexact(bufs[k][2].cpu().numpy(), o2["out_S"], f"pair {k} S o psi, 2nd call")
