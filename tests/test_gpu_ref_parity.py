@@ -254,3 +254,53 @@ def test_field_ops_vs_oracle_and_reference(cuda):
         assert_bitexact(got, O.interpolate_field(field, pos), f"interpolate_field {name}")
         if ref_runner.available():
             assert_bitexact(got, ref_runner.interpolate_gradient(field, pos), f"interpolate vs reference {name}")
+
+
+@pytest.mark.parametrize("kw", [dict(p=1.5, C=0.5, tau=0.1, rho_0=0.8, w_reg=0.05, alpha=0.03),
+                                dict(p=3.0, C=0.1, tau=0.35, rho_0=1.3, w_reg=0.6, alpha=0.01)])
+def test_nondefault_solver_constants(cuda, kw):
+    """Other values of the params.ini constants (the t^(p-2) factor below and above 1,
+    density start, diffusion and regularisation weights): a registration bit for bit."""
+    dims = (21, 19, 17)
+    d = images(dims, 77)
+    P = _params(dims, max_iter=30, **kw)
+    fr = FastReg(P)
+    iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
+    fr(iT, lT, iS, lS)
+    o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
+    norms, vox = fr.trace()
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI).cpu().numpy(), o["psi"], "psi")
+    assert_bitexact(fr.get_field(N.FR_FIELD_PSI_INV).cpu().numpy(), o["psi_inv"], "psi_inv")
+    assert_bitexact(fr.get_field(N.FR_FIELD_RHO).cpu().numpy(), o["rho"], "rho")
+    assert_bitexact(iS.cpu().numpy(), o["out_S"], "S o psi")
+    assert_bitexact(iT.cpu().numpy(), o["out_T"], "T o psi_inv")
+    assert_bitexact(norms, o["trace_norm"], "max update norms")
+    fr.close()
+
+
+def test_two_handles_interleaved(cuda):
+    """Two handles of different sizes and solvers used alternately, each on its own
+    stream: every call gives the oracle's bits (no state, graph or tuned shape leaks
+    between handles)."""
+    import torch
+    da, db = (19, 13, 11), (26, 22, 14)
+    pa, pb = images(da, 501), images(db, 502)
+    Pa = _params(da, max_iter=12, alpha=0.02)
+    Pb = Params(volume_dims=db, no_labels=4, max_iter=10, solver="sobolev", smooth_sigma=1.5, smooth_width=7,
+                damping=0.9, step=0.5)
+    oa = O.ref_register(Pa, pa["T"], pa["labT"], pa["S"], pa["labS"])
+    ob = O.sob_register(Pb, pb["T"], pb["S"])
+    fa, fb = FastReg(Pa), FastReg(Pb)
+    sa, sb = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(2):
+        ba = [_to(cuda, pa[k]) for k in ("T", "labT", "S", "labS")]
+        bb = [_to(cuda, pb[k]) for k in ("T", "labT", "S", "labS")]
+        torch.cuda.synchronize()
+        fa(*ba, stream=sa)
+        fb(*bb, stream=sb)
+        torch.cuda.synchronize()
+        assert_bitexact(fa.get_field(N.FR_FIELD_PSI).cpu().numpy(), oa["psi"], "reference handle psi")
+        assert_bitexact(ba[2].cpu().numpy(), oa["out_S"], "reference handle S o psi")
+        assert_bitexact(fb.get_field(N.FR_FIELD_PSI).cpu().numpy(), ob["phi"], "sobolev handle phi")
+    fa.close()
+    fb.close()
