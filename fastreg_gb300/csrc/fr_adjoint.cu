@@ -128,7 +128,9 @@ __global__ void adj_fwd_grad_kernel(AdjDims D, const float* __restrict__ S, cons
     }
 }
 
-// one separable pass (fma taps, replicate boundary); momentum: dst = damping*dst - step*acc
+// one separable pass of radius R (fma taps, replicate boundary); momentum: dst =
+// damping*dst - step*acc
+template <int R>
 __global__ void adj_fwd_smooth_kernel(AdjDims D, SobIterArgs a, int axis, const float* __restrict__ src, float* dst,
                                       int momentum) {
     const int dim = axis == 0 ? D.X : (axis == 1 ? D.Y : D.Z);
@@ -141,9 +143,10 @@ __global__ void adj_fwd_smooth_kernel(AdjDims D, SobIterArgs a, int axis, const 
         for (int c = 0; c < 3; ++c) {
             const float* Sp = src + (long long)c * D.N;
             float acc = 0.f;
-            for (int k = -a.radius; k <= a.radius; ++k) {
+#pragma unroll
+            for (int k = -R; k <= R; ++k) {
                 const int q = min(max(pos + k, 0), dim - 1);
-                acc = fmaf(a.taps[k + a.radius], __ldg(Sp + i + (q - pos) * stride), acc);
+                acc = fmaf(a.taps[k + R], __ldg(Sp + i + (q - pos) * stride), acc);
             }
             float* dp = dst + (long long)c * D.N + i;
             *dp = momentum ? a.damping * *dp - a.step * acc : acc;
@@ -219,24 +222,41 @@ __global__ void adj_momentum_kernel(AdjDims D, float damping, float step, float*
     }
 }
 
-// transpose of one replicate-boundary pass, gather form: dst(y) = sum over x of
-// src(x) * sum_k w_k [clamp(x + k) == y]
+// transpose of one replicate-boundary pass of radius R, gather form: dst(y) = sum over x
+// of src(x) * sum_k w_k [clamp(x + k) == y]
+template <int R>
 __global__ void adj_smooth_t_kernel(AdjDims D, SobIterArgs a, int axis, const float* __restrict__ src, float* dst) {
     const int dim = axis == 0 ? D.X : (axis == 1 ? D.Y : D.Z);
     const int stride = axis == 0 ? 1 : (axis == 1 ? D.X : D.XY);
-    const int R = a.radius;
     GRID_STRIDE(i, D.N) {
         int x, y, z;
         coords(D, i, x, y, z);
         const int pos = axis == 0 ? x : (axis == 1 ? y : z);
         float acc[3] = {0.f, 0.f, 0.f};
-        for (int s = max(pos - R, 0); s <= min(pos + R, dim - 1); ++s) {
-            float w = 0.f;
-            for (int k = -R; k <= R; ++k)
-                if (min(max(s + k, 0), dim - 1) == pos) w += a.taps[k + R];
-            if (w == 0.f) continue;
+        if (pos >= R && pos <= dim - 1 - R) {
+            // clamped taps land only on the first and last position: inside, the weight of
+            // s = pos + j is the single tap at -j (the sum below with one nonzero term)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) acc[c] += w * __ldg(src + (long long)c * D.N + i + (s - pos) * stride);
+            for (int j = -R; j <= R; ++j) {
+                const float w = a.taps[R - j];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[c] += w * __ldg(src + (long long)c * D.N + i + j * stride);
+            }
+        } else if (pos >= 1 && pos <= dim - 2) {
+            for (int s = max(pos - R, 0); s <= min(pos + R, dim - 1); ++s) {
+                const float w = a.taps[pos - s + R];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[c] += w * __ldg(src + (long long)c * D.N + i + (s - pos) * stride);
+            }
+        } else {
+            for (int s = max(pos - R, 0); s <= min(pos + R, dim - 1); ++s) {
+                float w = 0.f;
+                for (int k = -R; k <= R; ++k)
+                    if (min(max(s + k, 0), dim - 1) == pos) w += a.taps[k + R];
+                if (w == 0.f) continue;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[c] += w * __ldg(src + (long long)c * D.N + i + (s - pos) * stride);
+            }
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) dst[(long long)c * D.N + i] = acc[c];
@@ -285,6 +305,30 @@ __global__ void adj_identity_kernel(AdjDims D, float* phi) {
         phi[i] = (float)x;
         phi[D.N + i] = (float)y;
         phi[2 * D.N + i] = (float)z;
+    }
+}
+
+// one separable pass (transposed: the adjoint's) with the radius as a template argument
+template <int R>
+void launch_smooth_r(bool transposed, int grid, cudaStream_t s, const AdjDims& D, const SobIterArgs& a, int axis,
+                     const float* src, float* dst, int momentum) {
+    if (transposed)
+        adj_smooth_t_kernel<R><<<grid, 256, 0, s>>>(D, a, axis, src, dst);
+    else
+        adj_fwd_smooth_kernel<R><<<grid, 256, 0, s>>>(D, a, axis, src, dst, momentum);
+}
+
+void launch_smooth(int radius, bool transposed, int grid, cudaStream_t s, const AdjDims& D, const SobIterArgs& a,
+                   int axis, const float* src, float* dst, int momentum) {
+    switch (radius) {
+        case 0: launch_smooth_r<0>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 1: launch_smooth_r<1>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 2: launch_smooth_r<2>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 3: launch_smooth_r<3>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 4: launch_smooth_r<4>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 5: launch_smooth_r<5>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        case 6: launch_smooth_r<6>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
+        default: launch_smooth_r<7>(transposed, grid, s, D, a, axis, src, dst, momentum); break;
     }
 }
 
@@ -365,9 +409,9 @@ extern "C" int fr_sobolev_loss_grad(const float* d_T, const float* d_S, const in
     int rc = FR_OK;
     auto fwd_step = [&]() {
         adj_fwd_grad_kernel<<<grid, 256, 0, s>>>(D, d_S, d_T, phi, lambda, g);
-        adj_fwd_smooth_kernel<<<grid, 256, 0, s>>>(D, a, 0, g, tmp, 0);
-        adj_fwd_smooth_kernel<<<grid, 256, 0, s>>>(D, a, 1, tmp, g, 0);
-        adj_fwd_smooth_kernel<<<grid, 256, 0, s>>>(D, a, 2, g, m, 1);
+        launch_smooth(a.radius, false, grid, s, D, a, 0, g, tmp, 0);
+        launch_smooth(a.radius, false, grid, s, D, a, 1, tmp, g, 0);
+        launch_smooth(a.radius, false, grid, s, D, a, 2, g, m, 1);
         adj_fwd_update_kernel<<<grid, 256, 0, s>>>(D, m, phi);
     };
     auto copy = [&](float* dst, const float* src) {
@@ -402,9 +446,9 @@ extern "C" int fr_sobolev_loss_grad(const float* d_T, const float* d_S, const in
                 const float* mn = seg + N3 * (2 * (k - s0) + 1);
                 adj_update_kernel<<<grid, 256, 0, s>>>(D, phik, mn, pbar, pbar_k, mbar);
                 adj_momentum_kernel<<<grid, 256, 0, s>>>(D, damping, step, mbar, g);
-                adj_smooth_t_kernel<<<grid, 256, 0, s>>>(D, a, 2, g, tmp);
-                adj_smooth_t_kernel<<<grid, 256, 0, s>>>(D, a, 1, tmp, g);
-                adj_smooth_t_kernel<<<grid, 256, 0, s>>>(D, a, 0, g, gbar);
+                launch_smooth(a.radius, true, grid, s, D, a, 2, g, tmp, 0);
+                launch_smooth(a.radius, true, grid, s, D, a, 1, tmp, g, 0);
+                launch_smooth(a.radius, true, grid, s, D, a, 0, g, gbar, 0);
                 adj_grad_kernel<<<grid, 256, 0, s>>>(D, d_S, d_T, phik, lambda, gbar, pbar_k, dd + 1);
                 std::swap(pbar, pbar_k);
             }
