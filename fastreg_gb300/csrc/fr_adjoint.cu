@@ -20,6 +20,7 @@
 
 #include "../../include/fastreg_gb300.h"
 #include "fr_common.cuh"
+#include "fr_limits.h"
 #include "fr_sob.h"
 
 namespace frg {
@@ -501,8 +502,8 @@ extern "C" int fr_warp_adjoint(const float* d_pos, const float* d_img, const flo
         set_global_error("fr_warp_adjoint: NULL argument");
         return FR_ERR_INVALID_ARG;
     }
-    if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || (long long)dims[0] * dims[1] * dims[2] > (1LL << 31) - 1) {
-        set_global_error("fr_warp_adjoint: invalid dims");
+    if (dims[0] < 2 || dims[1] < 2 || dims[2] < 2 || !frg::fits_index32(dims[0], dims[1], dims[2])) {
+        set_global_error("fr_warp_adjoint: invalid dims (each >= 2, N + 2 X Y + 2 X + 2 <= 2^31-1)");
         return FR_ERR_INVALID_ARG;
     }
     AdjDims D{dims[0], dims[1], dims[2], dims[0] * dims[1], dims[0] * dims[1] * dims[2]};

@@ -20,6 +20,7 @@
 
 #include "../../include/fastreg_gb300.h"
 #include "fr_kernels.h"
+#include "fr_limits.h"
 #include "fr_sob.h"
 
 #include <chrono>
@@ -287,9 +288,11 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
                             pairs[p].dims[c]);
             dims[p][c] = pairs[p].dims[c];
         }
-        const long long Np = (long long)((dims[p][0] + 3) / 4 * 4) * dims[p][1] * dims[p][2];
-        if (Np > 0x7fffffffLL)
-            return fail(h, FR_ERR_INVALID_ARG, "pair %d is too large (%lld padded voxels, limit 2^31-1)", p, Np);
+        const long long Xp = (dims[p][0] + 3) / 4 * 4, Np = Xp * dims[p][1] * dims[p][2];
+        if (!frg::fits_index32(Xp, dims[p][1], dims[p][2]))
+            return fail(h, FR_ERR_INVALID_ARG,
+                        "pair %d is too large (%lld padded voxels: the kernels' 32-bit offsets need "
+                        "N + 2 X Y + 2 X + 2 <= 2^31-1)", p, Np);
     }
     const int want_trace = std::max(h->P.max_iter, 1);
     if (h->block && dims == h->dims && h->trace_cap >= want_trace) return FR_OK;
@@ -1331,7 +1334,7 @@ int fr_warp(const float* d_pos, const float* d_img, const int16_t* d_lab, const 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto aligned = [](const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; };
-    const bool vec4 = P.N % 4 == 0 && P.N <= 0x7fffffffLL && aligned(d_pos, 16) && aligned(d_out, 16) &&
+    const bool vec4 = P.N % 4 == 0 && frg::fits_index32(P.X, P.Y, P.Z) && aligned(d_pos, 16) && aligned(d_out, 16) &&
                       (!d_out_lab || aligned(d_out_lab, 8));
     const void* fn = vec4 ? (const void*)frg::warp4_kernel : (const void*)frg::warp_kernel;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
@@ -1355,8 +1358,8 @@ static int field_op_check(const void* a, const void* b, const void* c, const int
         g_parse_error = std::string(who) + ": NULL argument";
         return FR_ERR_INVALID_ARG;
     }
-    if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1 || (long long)dims[0] * dims[1] * dims[2] > 0x7fffffffLL) {
-        g_parse_error = std::string(who) + ": dims must be >= 1 with at most 2^31-1 voxels";
+    if (!frg::fits_index32(dims[0], dims[1], dims[2])) {
+        g_parse_error = std::string(who) + ": dims must be >= 1 with N + 2 X Y + 2 X + 2 <= 2^31-1";
         return FR_ERR_INVALID_ARG;
     }
     return FR_OK;

@@ -8,8 +8,12 @@
 // real-time pipeline that forbids allocation after start-up, or code running where
 // an allocation would synchronise the device.  For them the per-block partial sums
 // and the Dice bins live in one file-scope __device__ array, g_stats_scratch, of a
-// fixed size (FR_NOALLOC_SCRATCH_BYTES = 28,712 bytes) that every GPU loading this
-// library keeps until the process exits.  The function allocates nothing.
+// fixed size (FR_NOALLOC_SCRATCH_BYTES = 28,712 bytes).  The function allocates
+// nothing.  Its first call on a device looks up the array's device address; with CUDA's
+// lazy module loading that lookup loads this file's module onto the device (which may
+// allocate device memory once), so callers make that first call at start-up.  The array
+// then stays on the device until the process exits; the address is kept per device and
+// is not looked up again, so the function is not for use after cudaDeviceReset.
 //
 // The array is shared by every call: each call clears what must start at zero, and
 // calls whose work overlaps on the GPU (different streams, or different host

@@ -200,13 +200,19 @@ int fr_warp_adjoint(const float *d_pos, const float *d_img, const float *d_wbar,
  * computed from buffers the caller holds -- the original target d_T and its labels
  * d_labT, the warped source d_warped_S / d_warped_labS (S o psi) and psi (3 planes of
  * N positions) -- and written to the host struct *out (other fields zeroed).
- * Its scratch is one file-scope __device__ array of FR_NOALLOC_SCRATCH_BYTES that every
- * GPU loading this library keeps until exit; the function allocates nothing.  The
- * first call on a device looks up that array's device address (make it before any
- * stream capture).  Calls share the array: calls that overlap on the GPU race and must
- * be serialised by the caller.  Limits: dims >= 2, N <= FR_NOALLOC_MAX_VOXELS,
+ * Its scratch is one file-scope __device__ array of FR_NOALLOC_SCRATCH_BYTES; the
+ * function allocates nothing and calls no allocating routine.  The first call on a
+ * device is its set-up: it looks up that array's device address, and under CUDA's lazy
+ * module loading (the default) that lookup is what loads the array's module onto the
+ * device, which may allocate device memory once.  So make the first call on each device
+ * at start-up, while allocation is still allowed; from the second call on nothing is
+ * allocated, and the array stays on the device until the process exits.  The address is
+ * kept per device for the life of the process: do not use this function on a device
+ * after cudaDeviceReset.  Calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller.  Limits: dims >= 2, N <= FR_NOALLOC_MAX_VOXELS,
  * no_labels <= FR_MAX_LABELS; larger inputs return FR_ERR_INVALID_ARG with a message
- * in fr_last_error(NULL).  The call synchronises `stream`. */
+ * in fr_last_error(NULL).  The call copies its results to the host and synchronises
+ * `stream`, so it cannot be called while `stream` is being captured into a graph. */
 #define FR_NOALLOC_SCRATCH_BYTES 28712
 #define FR_NOALLOC_MAX_VOXELS 2147483647LL
 int fr_stats_noalloc(const float *d_T, const int16_t *d_labT, const float *d_warped_S, const int16_t *d_warped_labS,

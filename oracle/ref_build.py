@@ -2,7 +2,9 @@
 
 The five unmodified translation units src/fastreg/cuda/{solver,vector_fields,
 reductor,scalar_fields,volume}.cu of the reference are compiled where they lie
-(under /root/reference, read-only) with the reference's own nvcc flags
+(read-only; the tree named by the FASTREG_REFERENCE environment variable, by
+default the directory `reference` beside this repository) with the reference's own
+nvcc flags
 (CMakeLists.txt:39-46: --ftz=true --prec-div=false --prec-sqrt=false
 --expt-relaxed-constexpr), retargeted to sm_103a, into oracle/_ref/*.cubin.  Only
 device code is built: the host side of the reference loop (estimate_psi,
@@ -20,7 +22,7 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF = Path(os.environ.get("FASTREG_REFERENCE", "/root/reference"))
+REF = Path(os.environ.get("FASTREG_REFERENCE", str(HERE.parent.parent / "reference")))
 OUT = HERE / "_ref"
 UNITS = ("solver", "vector_fields", "reductor", "scalar_fields", "volume")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "--ftz=true", "--prec-div=false", "--prec-sqrt=false",

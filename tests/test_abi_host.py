@@ -180,3 +180,46 @@ def test_cpp_shim_compiles_and_runs(tmp_path):
         assert f"error {N.FR_ERR_CUDA}" in out.stdout
     else:
         assert "created" in out.stdout
+
+
+LIMITS_CHECK = r'''
+#include <cstdio>
+#include <initializer_list>
+#include "fr_limits.h"
+int main() {
+    const long long M = frg::kIndex32Max;
+    int bad = 0;
+    auto want = [&](long long X, long long Y, long long Z, bool ok) {
+        if (frg::fits_index32(X, Y, Z) != ok) { std::printf("wrong: %lld %lld %lld\n", X, Y, Z); ++bad; }
+    };
+    // the largest volume of pitch X and Y rows whose far-corner and prefetch offsets fit
+    for (long long X : {4LL, 184LL, 1024LL, 2048LL})
+        for (long long Y : {1LL, 218LL, 1024LL}) {
+            const long long XY = X * Y, Zmax = (M - 2 * XY - 2 * X - 2) / XY;
+            want(X, Y, Zmax, true);
+            want(X, Y, Zmax + 1, false);
+        }
+    want(184, 218, 182, true);
+    want(0, 5, 5, false);
+    want(1LL << 20, 1LL << 20, 1LL << 20, false);   // X*Y*Z overflows 64-bit arithmetic checks
+    want(46341, 46341, 1, false);                   // X*Y alone above 2^31 - 1
+    std::printf(bad ? "FAIL\n" : "OK\n");
+    return bad;
+}
+'''
+
+
+def test_index32_predicate(tmp_path):
+    """The 32-bit kernels take a volume only when its largest corner and prefetch
+    offset (N + 2 X Y + 2 X + 2) fits an int: the predicate at its boundary."""
+    import shutil
+    if shutil.which("g++") is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "limits.cpp"
+    src.write_text(LIMITS_CHECK)
+    exe = tmp_path / "limits"
+    subprocess.run(["g++", "-std=c++17", "-O1", str(src), "-o", str(exe), "-I",
+                    str(ROOT / "fastreg_gb300" / "csrc")], check=True, capture_output=True, text=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and "OK" in out.stdout, out.stdout
+
