@@ -8,9 +8,11 @@ in HBM.  Prints one JSON line.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference algorithm's CPU implementation (the oracle
-port, OpenMP over all host cores) on a bounded sample of the same workload.
+port, OpenMP over all host cores): one whole registration of the same pair per step;
+its line also carries the reference's own CUDA kernels timed on the same pair.
 Multi-GPU runs are independent replicas (one pair per rank, no collective on the
-data path); rank 0 prints.
+data path), and the shared-target cohort is split across the ranks by voxel count, one
+batched call per rank; rank 0 prints.
 """
 from __future__ import annotations
 
@@ -145,21 +147,41 @@ def allmax(ws, v):
     return max_over_ranks(v)
 
 
-def cpu_reference_sample(data, P, sample_iters=(2, 6)):
-    """Time the oracle port (the reference algorithm on the host cores) on the full
-    volume for a few iterations and extrapolate to a whole registration."""
+def cpu_registrations(data, P, n):
+    """Time `n` whole registrations of the pair by the oracle port (the reference
+    algorithm, FP32, OpenMP over the host cores); returns the seconds of each."""
     from oracle import oracle as O
-    a, b = sample_iters
-    times = {}
-    for n in (a, b):
-        Pn = reference_params(DIMS, n)
+    times = []
+    for _ in range(n):
         t0 = time.perf_counter()
-        O.ref_register(Pn, data["T"], data["labT"], data["S"], data["labS"])
-        times[n] = time.perf_counter() - t0
-    per_iter = max((times[b] - times[a]) / (b - a), 1e-9)
-    fixed = max(times[a] - a * per_iter, 0.0)
-    full = fixed + ITERS * per_iter
-    return 1.0 / full, per_iter, times
+        O.ref_register(P, data["T"], data["labT"], data["S"], data["labS"])
+        times.append(time.perf_counter() - t0)
+    return times
+
+
+def reference_cuda_timing(data, reps=3):
+    """The reference's own CUDA kernels (compiled unmodified from its sources for sm_103a,
+    launched in the order of its host code by the reference runner) on the same pair and
+    settings: device time of the whole FastReg::operator() sequence and of estimate_psi
+    alone, as the reference app times it (src/apps/demo.cpp:306-310).  None when the
+    reference kernels are not built or there is no GPU."""
+    try:
+        import torch
+        from oracle import ref_runner
+        if not (torch.cuda.is_available() and ref_runner.available()):
+            return None
+        P = reference_params()
+        runs = [ref_runner.register(P, data["T"], data["labT"], data["S"], data["labS"], timing=True)
+                for _ in range(reps + 1)][1:]
+    except Exception as e:  # the runner is test infrastructure: report, do not fail the line
+        return {"unavailable": f"{type(e).__name__}: {e}"[:200]}
+    op = [r["ms_operator"] for r in runs]
+    ep = [r["ms_estimate_psi"] for r in runs]
+    return {"what": "the reference's CUDA kernels built from its sources for sm_103a (its own nvcc flags), launched "
+                    "in its order: 13 launches and 2 host synchronisations per iteration",
+            "workload": "one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
+            "ms_operator": statistics.median(op), "ms_estimate_psi": statistics.median(ep),
+            "pairs_per_s": 1000.0 / statistics.median(op), "runs": reps, "ms_operator_all": op}
 
 
 def run_reference_arm(args):
@@ -173,24 +195,26 @@ def run_reference_arm(args):
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
     data = sy.make_pair(sy.PAIR_182X218X182)
     P = reference_params()
-    vals = []
-    for step in range(args.warmup + args.steps):
-        v, per_iter, _ = cpu_reference_sample(data, P, sample_iters=(1, 2))
-        if step >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
+    # one step = one whole 200-iteration registration of the pair on the host cores
+    cpu_registrations(data, P, args.warmup)
+    times = cpu_registrations(data, P, args.steps)
+    total = sum(times)
+    value = args.steps / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "one 182x218x182 pair, 200 iterations, reference PDE solver (params.ini values)",
-                   "solver": "reference", "sample": "1 and 2 iterations of the full volume per step, extrapolated "
-                                                   "to 200 iterations"},
+                   "solver": "reference", "sample": "each step is one whole 200-iteration registration"},
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
-                         "sample": "CPU oracle (OpenMP, FP32, op-order matched) on the 182x218x182 pair, 1 and 2 "
-                                   "iterations, extrapolated to 200"},
+                         "sample": "CPU oracle (OpenMP, FP32, op-order matched): whole 200-iteration registrations "
+                                   "of the 182x218x182 pair, one per step"},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_s": [round(t, 3) for t in times],
     }
+    ref_cuda = reference_cuda_timing(data)
+    if ref_cuda is not None:
+        line["reference_cuda"] = ref_cuda
     print(json.dumps(line))
     return 0
 
@@ -230,6 +254,7 @@ def profile_case(args):
     dev = torch.device("cuda", 0)
     data = sy.make_pair(sy.PAIR_182X218X182)
     P = reference_params(DIMS, args.iters, solver=args.solver)
+    P.staging = args.staging
     fr = FastReg(P)
     fresh = lambda: [torch.from_numpy(data[k]).to(dev) for k in ("T", "labT", "S", "labS")]  # noqa: E731
     fr(*fresh())
@@ -244,7 +269,8 @@ def profile_case(args):
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
     st = fr.stats()
-    print(f"profile case: {args.solver} solver, {st.iterations} iterations, e_data {st.e_data:.6g}")
+    print(f"profile case: {args.solver} solver, {st.iterations} iterations, e_data {st.e_data:.6g}, "
+          f"staging {fr.tile_staging()}, shapes {fr.tile_shapes()}")
     fr.close()
     return 0
 
@@ -303,53 +329,6 @@ def small_pair_timing(dev, stream, reps=5):
     return out
 
 
-def batched_vs_plain_shared(dev, stream, n_pairs=32):
-    """The shared-target cohort of 32 sources of 160x192x160 (reference solver, 200
-    iterations): one fr_register_batch against 32 fr_register calls on one handle; one
-    warm-up each, then one timed run each; the fields of the two are compared bit for bit."""
-    import torch
-    from fastreg_gb300 import FastReg, synthetic as sy, _native as N
-    pairs = sy.shared_target_cohort(n_pairs, device=dev)
-    pristine = [(d["T"], d["labT"], d["S"], d["labS"]) for d in pairs]
-    work = [tuple(t.clone() for t in q) for q in pristine]
-
-    def restore():
-        for w, p in zip(work, pristine):
-            for a, b in zip(w, p):
-                a.copy_(b, non_blocking=True)
-
-    dims = tuple(reversed(pristine[0][0].shape))
-    frb = FastReg(reference_params(dims=dims))
-    frp = FastReg(reference_params(dims=dims))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    times = {}
-    with torch.cuda.stream(stream):
-        for mode in ("batched", "plain"):
-            for rep in range(2):
-                restore()
-                e0.record(stream)
-                if mode == "batched":
-                    frb.register_batch(work, stream=stream, sync=False)
-                else:
-                    for w in work:
-                        frp(*w, stream=stream, sync=False)
-                e1.record(stream)
-                stream.synchronize()
-                times[mode] = e0.elapsed_time(e1)
-            if mode == "batched":
-                psi_b = [frb.get_field(N.FR_FIELD_PSI, pair=k) for k in (0, n_pairs - 1)]
-    same = torch.equal(psi_b[1], frp.get_field(N.FR_FIELD_PSI))  # the last pair of both runs
-    ssd_b, ssd_p = frb.stats(n_pairs - 1).e_data, frp.stats().e_data
-    frb.close()
-    frp.close()
-    return {"cohort": f"{n_pairs} sources of {dims[0]}x{dims[1]}x{dims[2]} to one shared target (velocity sigma 5, "
-                      "max displacement 5, N(0,0.02) noise, 8 classes), reference solver, 200 iterations",
-            "batched_pairs_per_s": n_pairs * 1000.0 / times["batched"],
-            "plain_pairs_per_s": n_pairs * 1000.0 / times["plain"],
-            "ratio": times["plain"] / times["batched"], "batched_ms": times["batched"], "plain_ms": times["plain"],
-            "bitexact_batched_vs_plain": bool(same), "final_ssd_rel_diff": abs(ssd_b - ssd_p) / max(abs(ssd_p), 1e-30)}
-
-
 def hypergradient_cohort(dev, stream, n_pairs=32):
     """The shared-target cohort (32 x 160x192x160): each pair's W_REG tuned by 5
     hypergradient steps through a 30-iteration unrolled sobolev registration (adjoint
@@ -381,27 +360,25 @@ def hypergradient_cohort(dev, stream, n_pairs=32):
     return out
 
 
-def batched_vs_plain(dev, stream, n_pairs=16, reps=2):
-    """One fr_register_batch over the uneven cohort against one fr_register per pair
-    (a handle per pair size), same data, same iterations; checks the two agree bit
-    for bit."""
+def batched_vs_plain(dev, stream, pristine, solver, what, reps=2):
+    """One fr_register_batch over a cohort against one fr_register per pair (a handle per
+    pair size), same data and iterations: one warm-up and `reps` timed runs of each mode
+    (CUDA events on `stream`, fastest run kept).  Then, untimed, every pair is registered
+    alone once more and compared with its batched result: psi, both warped images and
+    both warped label maps bit for bit, and the final SSD."""
     import torch
-    from fastreg_gb300 import FastReg, synthetic as sy, _native as N
-    specs = sy.cohort_specs(n_pairs)
-    pristine = []
-    for sp in specs:
-        d = sy.make_pair_torch(sp, dev)
-        pristine.append((d["T"], d["labT"], d["S"], d["labS"]))
+    from fastreg_gb300 import FastReg, _native as N
+    n = len(pristine)
     work = [tuple(t.clone() for t in q) for q in pristine]
+    dims = [tuple(reversed(q[0].shape)) for q in pristine]
 
-    def restore():
-        for w, p in zip(work, pristine):
-            for a, b in zip(w, p):
-                a.copy_(b, non_blocking=True)
+    def restore(k=None):
+        for j in (range(n) if k is None else [k]):
+            for a_, b_ in zip(work[j], pristine[j]):
+                a_.copy_(b_, non_blocking=True)
 
-    P = reference_params(dims=specs[0].dims)
-    frb = FastReg(P)
-    plain = [FastReg(reference_params(dims=sp.dims)) for sp in specs]
+    frb = FastReg(reference_params(dims=dims[0], solver=solver))
+    plain = {d: FastReg(reference_params(dims=d, solver=solver)) for d in sorted(set(dims))}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     tb, tp = [], []
     with torch.cuda.stream(stream):
@@ -413,32 +390,131 @@ def batched_vs_plain(dev, stream, n_pairs=16, reps=2):
             stream.synchronize()
             if rep:
                 tb.append(e0.elapsed_time(e1))
-        psi_b = [frb.get_field(N.FR_FIELD_PSI, pair=k) for k in range(n_pairs)]
-        lab_b = [w[3].clone() for w in work]
+        out_b = [(frb.get_field(N.FR_FIELD_PSI, pair=k),) + tuple(t.clone() for t in work[k]) for k in range(n)]
+        ssd_b = [frb.stats(k).e_data for k in range(n)]
         for rep in range(reps + 1):
             restore()
             e0.record(stream)
-            for fr, w in zip(plain, work):
-                fr(*w, stream=stream, sync=False)
+            for k in range(n):
+                plain[dims[k]](*work[k], stream=stream, sync=False)
             e1.record(stream)
             stream.synchronize()
             if rep:
                 tp.append(e0.elapsed_time(e1))
-    same = all(torch.equal(psi_b[k], plain[k].get_field(N.FR_FIELD_PSI)) and torch.equal(lab_b[k], work[k][3])
-               for k in range(n_pairs))
-    ssd_b = [frb.stats(k).e_data for k in range(n_pairs)]
-    ssd_p = [plain[k].stats().e_data for k in range(n_pairs)]
-    voxels = sum(sp.dims[0] * sp.dims[1] * sp.dims[2] for sp in specs)
-    t_b, t_p = min(tb), min(tp)
-    for fr in plain:
+        names = ("psi", "T o psi_inv", "labels T", "S o psi", "labels S")
+        mismatch = {}
+        ssd_rel = []
+        for k in range(n):  # every pair alone, against its batched result
+            restore(k)
+            fr = plain[dims[k]]
+            fr(*work[k], stream=stream, sync=False)
+            stream.synchronize()
+            got = (fr.get_field(N.FR_FIELD_PSI),) + tuple(work[k])
+            for nm, x, y in zip(names, got, out_b[k]):
+                if not torch.equal(x, y):
+                    mismatch.setdefault(nm, []).append(k)
+            e = fr.stats().e_data
+            ssd_rel.append(abs(ssd_b[k] - e) / max(abs(e), 1e-30))
+    for fr in plain.values():
         fr.close()
     frb.close()
-    return {"cohort": f"{n_pairs} pairs, dims per pair from {{96,128,160,192}}x{{112,160,224}}x{{96,128,192}}, "
-                      f"{voxels} voxels in total, reference solver, {ITERS} iterations",
-            "batched_pairs_per_s": n_pairs / (t_b / 1000.0), "plain_pairs_per_s": n_pairs / (t_p / 1000.0),
-            "ratio": t_p / t_b, "batched_ms": t_b, "plain_ms": t_p,
-            "bitexact_batched_vs_plain": bool(same),
-            "max_ssd_rel_diff": max(abs(a - b) / max(abs(b), 1e-30) for a, b in zip(ssd_b, ssd_p))}
+    t_b, t_p = min(tb), min(tp)
+    voxels = sum(d[0] * d[1] * d[2] for d in dims)
+    return {"cohort": what, "solver": solver, "pairs": n, "voxels": voxels, "iterations": ITERS,
+            "batched_pairs_per_s": n / (t_b / 1000.0), "plain_pairs_per_s": n / (t_p / 1000.0),
+            "ratio": t_p / t_b, "batched_ms": t_b, "plain_ms": t_p, "timed_runs": reps,
+            "bitexact_batched_vs_plain": not mismatch, "compared": "psi, both warped images and both warped label "
+                                                                  "maps of every pair",
+            "mismatches": mismatch, "max_final_ssd_rel_diff": max(ssd_rel)}
+
+
+def staging_variants(dev, stream, pristine, iters=20):
+    """Per-kernel times of both solvers on the bench pair with each staging forced
+    (STAGING=1: per-thread cp.async, STAGING=2: TMA tensor copies where a kernel has
+    them), each with its own autotuned tile shapes: CUDA events around every launch of
+    `iters` iterations (fr_time_kernels), after one registration."""
+    import ctypes as C
+    from fastreg_gb300 import FastReg, _native as N
+    names = {"reference": ["ref_laplacian_kernel", "ref_pass_a_kernel", "ref_pass_b_kernel"],
+             "sobolev": ["sob_grad_kernel", "sob_smooth3_kernel", "sob_pass_b_kernel"]}
+    out = {}
+    work = [t.clone() for t in pristine]
+    for solver in ("reference", "sobolev"):
+        for staging in (1, 2):
+            P = reference_params(solver=solver)
+            P.staging = staging
+            fr = FastReg(P)
+            for w, p in zip(work, pristine):
+                w.copy_(p)
+            fr(*work, stream=stream)
+            fr.begin([tuple(work)], stream=stream)
+            ms = (C.c_float * 8)()
+            nk = C.c_int()
+            N.check(fr.lib.fr_time_kernels(fr.h, iters, ms, C.byref(nk), stream.cuda_stream), fr.h,
+                    "fr_time_kernels")
+            stream.synchronize()
+            out[f"{solver}_staging{staging}"] = {
+                "kernels_ms": {n: ms[k] for k, n in enumerate(names[solver])},
+                "staging": fr.tile_staging(), "tile_shapes": fr.tile_shapes()}
+            fr.close()
+    return out
+
+
+def sharded_cohort(dev, stream, ws, rank, reps=2):
+    """Replicas over several GPUs: the shared-target cohort (32 x 160x192x160, sobolev
+    solver) split across the ranks by voxel count (replicas.shard_pairs), one
+    fr_register_batch per rank over its pairs; the job's time is the slowest rank's
+    (barrier before, max over ranks after); per-pair statistics gathered on rank 0."""
+    import torch
+    from fastreg_gb300 import FastReg, synthetic as sy
+    from fastreg_gb300.replicas import gather_to_rank0, shard_pairs
+    n, dims = 32, (160, 192, 160)
+    mine = shard_pairs([dims[0] * dims[1] * dims[2]] * n, ws)[rank]
+    cohort = sy.shared_target_cohort(n, dims=dims, device=dev)
+    pristine = [(cohort[k]["T"], cohort[k]["labT"], cohort[k]["S"], cohort[k]["labS"]) for k in mine]
+    work = [tuple(t.clone() for t in q) for q in pristine]
+    fr = FastReg(reference_params(dims=dims, solver="sobolev"))
+    times = []
+    with torch.cuda.stream(stream):
+        for rep in range(reps + 1):
+            for w, p in zip(work, pristine):
+                for a_, b_ in zip(w, p):
+                    a_.copy_(b_, non_blocking=True)
+            stream.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+            fr.register_batch(work, stream=stream, sync=False)
+            stream.synchronize()
+            dt = allmax(ws, time.perf_counter() - t0)
+            if rep:
+                times.append(dt)
+    stats = gather_to_rank0([(k, fr.stats(j).e_data) for j, k in enumerate(mine)])
+    fr.close()
+    t = min(times)
+    return {"cohort": f"{n} sources of 160x192x160 to one shared target, sobolev solver, {ITERS} iterations",
+            "ranks": ws, "pairs_per_rank": [len(x) for x in shard_pairs([1] * n, ws)], "seconds": t,
+            "pairs_per_s": n / t, "e_data": sorted(x for r in (stats or []) for x in r) if stats else None}
+
+
+def cohort_blocks(dev, stream):
+    """The two cohorts with a batched target: the 16 uneven pairs and the 32 sources of
+    160x192x160 registered to one shared target, each with both solvers."""
+    from fastreg_gb300 import synthetic as sy
+    specs = sy.cohort_specs(16)
+    mixed = []
+    for sp in specs:
+        d = sy.make_pair_torch(sp, dev)
+        mixed.append((d["T"], d["labT"], d["S"], d["labS"]))
+    shared = [(d["T"], d["labT"], d["S"], d["labS"]) for d in sy.shared_target_cohort(32, device=dev)]
+    w_mixed = ("16 pairs, dims per pair from {96,128,160,192}x{112,160,224}x{96,128,192}, max displacement "
+               "2-6 voxels")
+    w_shared = ("32 sources of 160x192x160 to one shared target (velocity sigma 5, max displacement 5, N(0,0.02) "
+                "noise, 8 classes)")
+    out = {}
+    for solver in ("sobolev", "reference"):
+        out[f"mixed_{solver}"] = batched_vs_plain(dev, stream, mixed, solver, w_mixed)
+        out[f"shared_target_{solver}"] = batched_vs_plain(dev, stream, shared, solver, w_shared)
+    return out
 
 
 def main():
@@ -454,6 +530,8 @@ def main():
     ap.add_argument("--iters", type=int, default=ITERS, help="iterations of the --profile registration")
     ap.add_argument("--solver", default="reference", choices=["reference", "sobolev", "adjoint"],
                     help="solver of the --profile registration")
+    ap.add_argument("--staging", type=int, default=0, choices=[0, 1, 2],
+                    help="STAGING of the --profile registration (0: the autotuner's choice, 1: cp.async, 2: TMA)")
     args = ap.parse_args()
     if args.profile:
         return profile_case(args)
@@ -579,6 +657,10 @@ def main():
                         "autotune_s": max(0.0, t_first - t_next)},
     }
 
+    if ws > 1 and not args.no_extras:
+        # every rank takes part: its share of the shared-target cohort in one batched call
+        line["cohort_replicas"] = sharded_cohort(dev, stream, ws, rank)
+
     if rank == 0 and not args.no_extras and not args.profile:
         peak, peak_kind = load_peaks()
         # per-kernel durations (CUDA events around each launch on `stream`)
@@ -650,13 +732,16 @@ def main():
                            "folds": ss.folds, "dice_all": ss.dice_all}
         frs.close()
 
+        # each kernel with either staging of its stencil operands (cp.async / TMA)
+        line["staging_variants"] = staging_variants(dev, stream, pristine)
+
         # the 64^3 single-pair workload (the CPU-runnable configuration), both solvers
         line["pair_64cube"] = small_pair_timing(dev, stream)
 
-        # batched cohort against plain per-pair calls: 16 uneven pairs, 200 iterations each
-        line["batched"] = batched_vs_plain(dev, stream)
-        # the shared-target cohort the batched target is quoted on: 32 x 160x192x160
-        line["batched_shared_target"] = batched_vs_plain_shared(dev, stream)
+        # batched cohorts against plain per-pair calls, 200 iterations each, both solvers:
+        # 16 uneven pairs, and the shared-target cohort the batched target is quoted on
+        # (32 x 160x192x160)
+        line["batched"] = cohort_blocks(dev, stream)
         # the same cohort with per-pair weights tuned by hypergradients (adjoint kernels)
         line["hypergradient_cohort"] = hypergradient_cohort(dev, stream)
 
@@ -664,13 +749,14 @@ def main():
         # J = SSD + 0.1 |m_K|^2 with respect to v0 and lambda, checkpoints every 10
         line["adjoint"] = adjoint_timing(dev, stream)
 
-        # CPU baseline: the oracle port on the host cores, bounded sample
+        # CPU baseline: the oracle port on the host cores, bounded sample of two whole
+        # registrations (about 15 s of CPU work)
         cores = os.cpu_count() or 1
         os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-        cpu_v, per_iter, _ = cpu_reference_sample(data, P, sample_iters=(1, 3))
-        line["cpu_baseline"] = {"value": cpu_v, "unit": "pairs/s", "cores": cores, "kind": "port",
-                                "sample": "CPU oracle (OpenMP, FP32) on the 182x218x182 pair, 1 and 3 iterations, "
-                                          f"extrapolated to 200 ({per_iter * 1e3:.1f} ms/iteration)"}
+        ct = cpu_registrations(data, P, 2)
+        line["cpu_baseline"] = {"value": len(ct) / sum(ct), "unit": "pairs/s", "cores": cores, "kind": "port",
+                                "sample": "CPU oracle (OpenMP, FP32) on the 182x218x182 pair: two whole "
+                                          f"200-iteration registrations ({', '.join(f'{t:.2f}' for t in ct)} s)"}
 
     if rank == 0:
         print(json.dumps(line))

@@ -54,6 +54,7 @@ class fr_params(C.Structure):
         ("step", C.c_float),
         ("keep_state", C.c_int),
         ("autotune", C.c_int),
+        ("staging", C.c_int),
     ]
 
 
@@ -107,6 +108,7 @@ SIGNATURES = [
     ("fr_warp", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p, C.c_void_p]),
     ("fr_set_pair_w_reg", C.c_int, [C.c_void_p, C.c_void_p, C.c_int]),
     ("fr_tile_shape", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    ("fr_tile_staging", C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     ("fr_estimate_inverse", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_void_p]),
     ("fr_interpolate_field", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_void_p]),
     ("fr_sobolev_loss_grad", C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_float, C.c_int,

@@ -21,6 +21,7 @@
 #include "../../include/fastreg_gb300.h"
 #include "fr_kernels.h"
 #include "fr_limits.h"
+#include "fr_tma.cuh"
 #include "fr_sob.h"
 
 #include <chrono>
@@ -37,13 +38,14 @@ enum Role { R_LAP, R_PA, R_PB, R_SG, R_SS, R_SB, R_COUNT };
 struct Shape {
     int depth = 16;  // slices per tile
     int bps = 0;     // blocks per SM (-1: one block per tile, scheduled by the hardware)
+    int variant = 0; // 0: staging by per-thread cp.async; 1: by TMA tensor copies (kernels that have both)
 };
 struct TileSet {
     Shape shape;
     std::vector<Tile> h;
     Tile* d = nullptr;  // device copy (capacity cap tiles)
     size_t cap = 0;
-    int occ = 1;   // resident blocks per SM at the kernel's registers and shared memory
+    int occ[2] = {1, 1};  // resident blocks per SM of each variant at its registers and shared memory
     int grid = 0;
 };
 // defaults (AUTOTUNE=0), the autotuner's usual choice on the 182x218x182 pair: slices per
@@ -51,6 +53,7 @@ struct TileSet {
 // persistent grid at the occupancy limit
 static const int kDefaultDepth[R_COUNT] = {16, 24, 24, 12, 32, 8};
 static const bool kDefaultPerTile[R_COUNT] = {true, true, false, true, true, false};
+static const int kDefaultVariant[R_COUNT] = {0, 0, 0, 0, 0, 0};
 static const int kMinDepth = 1;  // thin tiles give small volumes enough blocks
 static const int kTuneWarmIters = 20;  // iterations run before the autotuner times shapes
 
@@ -86,6 +89,9 @@ struct fr_handle {
     unsigned long long* keys = nullptr;
     unsigned long long* trace = nullptr;
     unsigned int* counter = nullptr;
+    CUtensorMap* tmaps = nullptr;   // [npairs][TM_COUNT] tensor maps of the TMA-staged kernels
+    unsigned int* dev_err = nullptr;  // device error word of the staged kernels
+    bool tma_ok = false;            // the maps of this cohort are encoded (else only variant 0 runs)
     double* tile_partials = nullptr;
     long long* tile_folds = nullptr;
     unsigned long long* dice = nullptr;
@@ -192,6 +198,7 @@ int check_params(fr_handle* h, const fr_params* p) {
         if (!(p->smooth_sigma > 0.f)) return fail(h, FR_ERR_INVALID_ARG, "smooth_sigma must be > 0");
     }
     if (p->verbosity < 0 || p->verbosity > 2) return fail(h, FR_ERR_INVALID_ARG, "verbosity must be 0, 1 or 2");
+    if (p->staging < 0 || p->staging > 2) return fail(h, FR_ERR_INVALID_ARG, "staging must be 0, 1 or 2");
     return FR_OK;
 }
 
@@ -200,6 +207,17 @@ int occupancy_grid(fr_handle* h, const void* fn, int ntiles, size_t smem = 0) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
     long long g = (long long)per_sm * h->num_sms;
     return (int)std::max(1LL, std::min<long long>(g, ntiles));
+}
+
+// The staged kernels' error word (set when a bounded wait gave up); the caller has
+// synchronised the work that could set it.
+int check_device_error(fr_handle* h) {
+    if (!h->dev_err) return FR_OK;
+    unsigned int e = 0;
+    FR_CUDA(h, cudaMemcpy(&e, h->dev_err, sizeof e, cudaMemcpyDeviceToHost));
+    if (e & frg::kErrTmaTimeout)
+        return fail(h, FR_ERR_CUDA, "a TMA staging wait gave up after its time limit (device error word %u)", e);
+    return FR_OK;
 }
 
 void release(fr_handle* h) {
@@ -220,22 +238,32 @@ std::vector<int> active_roles(const fr_handle* h) {
     return {R_SG, R_SS, R_SB};
 }
 
-const void* role_fn(const fr_handle* h, int r) {
+// kernels with a TMA-staged variant
+bool has_tma_variant(int r) { return r == R_LAP || r == R_SG || r == R_SS; }
+
+// the staging variants kernel r may run with this handle's STAGING and cohort
+std::vector<int> allowed_variants(const fr_handle* h, int r) {
+    if (!has_tma_variant(r) || !h->tma_ok || h->P.staging == 1) return {0};
+    if (h->P.staging == 2) return {1};
+    return {0, 1};
+}
+
+const void* role_fn(const fr_handle* h, int r, int variant = 0) {
     switch (r) {
-        case R_LAP: return (const void*)frg::ref_laplacian_kernel;
+        case R_LAP: return variant ? (const void*)frg::ref_laplacian_tma_kernel : (const void*)frg::ref_laplacian_kernel;
         case R_PA: return (const void*)frg::ref_pass_a_kernel;
         case R_PB: return (const void*)frg::ref_pass_b_kernel;
-        case R_SG: return (const void*)frg::sob_grad_kernel;
-        case R_SS: return frg::sob_smooth3_fn(h->P.smooth_width / 2);
+        case R_SG: return variant ? (const void*)frg::sob_grad_tma_kernel : (const void*)frg::sob_grad_kernel;
+        case R_SS: return frg::sob_smooth3_fn(h->P.smooth_width / 2, variant);
         default: return (const void*)frg::sob_pass_b_kernel;
     }
 }
 
-size_t role_smem(int r) {
+size_t role_smem(int r, int variant = 0) {
     switch (r) {
-        case R_LAP: return frg::ref_laplacian_smem_bytes();
+        case R_LAP: return variant ? frg::ref_laplacian_tma_smem_bytes() : frg::ref_laplacian_smem_bytes();
         case R_PA: return frg::ref_pass_a_smem_bytes();
-        case R_SG: return frg::sob_grad_smem_bytes();
+        case R_SG: return variant ? frg::sob_grad_tma_smem_bytes() : frg::sob_grad_smem_bytes();
         default: return 0;
     }
 }
@@ -244,7 +272,11 @@ typedef std::array<Shape, R_COUNT> Shapes;
 
 Shapes default_shapes(const fr_handle* h) {
     Shapes sh{};
-    for (int r = 0; r < R_COUNT; ++r) sh[r] = Shape{kDefaultDepth[r], kDefaultPerTile[r] ? -1 : h->ts[r].occ};
+    for (int r = 0; r < R_COUNT; ++r) {
+        const std::vector<int> al = allowed_variants(h, r);
+        const int v = al.size() == 1 ? al[0] : kDefaultVariant[r];
+        sh[r] = Shape{kDefaultDepth[r], kDefaultPerTile[r] ? -1 : h->ts[r].occ[v], v};
+    }
     return sh;
 }
 
@@ -252,7 +284,11 @@ Shapes default_shapes(const fr_handle* h) {
 int build_role(fr_handle* h, int r, Shape sh, cudaStream_t s = 0) {
     TileSet& t = h->ts[r];
     sh.depth = std::max(sh.depth, kMinDepth);
-    if (sh.bps != -1) sh.bps = std::min(std::max(sh.bps, 1), t.occ);
+    {
+        const std::vector<int> al = allowed_variants(h, r);
+        if (std::find(al.begin(), al.end(), sh.variant) == al.end()) sh.variant = al[0];
+    }
+    if (sh.bps != -1) sh.bps = std::min(std::max(sh.bps, 1), t.occ[sh.variant]);
     t.shape = sh;
     t.h.clear();
     for (int p = 0; p < h->npairs; ++p) {
@@ -275,6 +311,77 @@ int apply_shapes(fr_handle* h, const Shapes& sh, cudaStream_t s = 0) {
         if (rc != FR_OK) return rc;
     }
     h->graph_valid = false;  // the captured launches carry the old tables
+    return FR_OK;
+}
+
+// ---- tensor maps of the TMA-staged kernels ----
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// cuTensorMapEncodeTiled from the driver, through the runtime (no link against libcuda)
+EncodeTiledFn encode_tiled_fn() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// A map of a float field of the packed layout: dims[0..rank) innermost first, byte
+// strides of dims 1..rank-1, the box copied per request; out-of-volume elements read 0.
+int encode_map(fr_handle* h, CUtensorMap* m, const float* base, int rank, const cuuint64_t* dims,
+               const cuuint64_t* strides, const cuuint32_t* box) {
+    EncodeTiledFn fn = encode_tiled_fn();
+    if (!fn) return fail(h, FR_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint32_t ones[5] = {1, 1, 1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, (void*)base, dims, strides, box, ones,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(h, FR_ERR_CUDA, "cuTensorMapEncodeTiled failed (CUresult %d)", (int)r);
+    return FR_OK;
+}
+
+// Every pair's maps (frg::TmapIndex), copied to the device.  Boxes: whole 16-byte chunks
+// along x starting at a multiple of 4 floats (the kernels' x coordinates are x0 - 4 or
+// x0, x0 a multiple of 32), so every copy starts on a 16-byte boundary.
+int encode_tmaps(fr_handle* h) {
+    std::vector<CUtensorMap> maps((size_t)h->npairs * frg::TM_COUNT);
+    const cuuint64_t fstride = sizeof(float) * (cuuint64_t)h->NT;  // component plane stride
+    for (int p = 0; p < h->npairs; ++p) {
+        const Pair& P = h->hpairs[p];
+        const cuuint64_t Xp = P.Xp, Y = P.Y, Z = P.Z;
+        CUtensorMap* m = maps.data() + (size_t)p * frg::TM_COUNT;
+        {
+            const cuuint64_t dims[4] = {Xp, Y, Z, 3}, strides[3] = {4 * Xp, 4 * Xp * Y, fstride};
+            const cuuint32_t box[4] = {40, 10, 1, 3};
+            int rc = encode_map(h, m + frg::TM_LAP_PSI, h->psi + P.off, 4, dims, strides, box);
+            if (rc != FR_OK) return rc;
+        }
+        {
+            const cuuint64_t dims[3] = {Xp, Y, Z}, strides[2] = {4 * Xp, 4 * Xp * Y};
+            const cuuint32_t box[3] = {32, 8, 1};
+            int rc = encode_map(h, m + frg::TM_LAP_T, h->T + P.off, 3, dims, strides, box);
+            if (rc != FR_OK) return rc;
+        }
+        if (h->P.solver == FR_SOLVER_SOBOLEV) {
+            int wx = 0, rows = 0;
+            frg::sob_smooth_box(h->P.smooth_width / 2, &wx, &rows);
+            const cuuint64_t dims[4] = {Xp, Y, Z, 3}, strides[3] = {4 * Xp, 4 * Xp * Y, fstride};
+            const cuuint32_t box[4] = {(cuuint32_t)wx, (cuuint32_t)rows, 1, 3};
+            int rc = encode_map(h, m + frg::TM_SOB_G, h->grad + P.off, 4, dims, strides, box);
+            if (rc != FR_OK) return rc;
+        }
+    }
+    FR_CUDA(h, cudaMemcpy(h->tmaps, maps.data(), sizeof(CUtensorMap) * maps.size(), cudaMemcpyHostToDevice));
     return FR_OK;
 }
 
@@ -364,6 +471,8 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     add((void**)&h->keys, sizeof(unsigned long long) * n);
     add((void**)&h->trace, sizeof(unsigned long long) * (size_t)n * want_trace);
     add((void**)&h->counter, sizeof(unsigned int) * 4);
+    add((void**)&h->dev_err, sizeof(unsigned int));
+    add((void**)&h->tmaps, sizeof(CUtensorMap) * (size_t)n * frg::TM_COUNT);
     add((void**)&h->tile_partials, sizeof(double) * 2 * ntiles);
     add((void**)&h->tile_folds, sizeof(long long) * ntiles);
     add((void**)&h->dice, sizeof(unsigned long long) * (size_t)n * (2 * 256 + 1));
@@ -395,13 +504,23 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
         FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)frg::ref_pass_a_smem_bytes()));
-    for (int r : active_roles(h)) {
-        int occ = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, role_fn(h, r), 256, role_smem(r)) != cudaSuccess ||
-            occ < 1)
-            occ = 1;
-        h->ts[r].occ = occ;
+    h->tma_ok = encode_tmaps(h) == FR_OK;
+    if (!h->tma_ok && h->P.staging == 2) {
+        const std::string why = h->err;
+        release(h);
+        return fail(h, FR_ERR_CUDA, "STAGING=2 asks for TMA staging, but the tensor maps could not be made (%s)",
+                    why.c_str());
     }
+    h->err.clear();  // a cohort whose maps cannot be encoded runs the cp.async variants
+    for (int r : active_roles(h))
+        for (int v = 0; v < (has_tma_variant(r) ? 2 : 1); ++v) {
+            int occ = 0;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, role_fn(h, r, v), 256, role_smem(r, v)) !=
+                    cudaSuccess ||
+                occ < 1)
+                occ = 1;
+            h->ts[r].occ[v] = occ;
+        }
     h->tuned = false;
     {
         int rc = apply_shapes(h, default_shapes(h));
@@ -451,13 +570,18 @@ frg::RefIterArgs ref_args(fr_handle* h, int iter, float t) {
     a.keys = h->keys;
     a.trace = h->trace;
     a.counter = h->counter;
+    a.tmaps = h->tmaps;
+    a.err = h->dev_err;
     return a;
 }
 
 int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev) {
     frg::RefIterArgs a = ref_args(h, iter, t);
     if (ev) cudaEventRecord(ev[0], s);
-    frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, frg::ref_laplacian_smem_bytes(), s>>>(a);
+    if (h->ts[R_LAP].shape.variant)
+        frg::ref_laplacian_tma_kernel<<<h->ts[R_LAP].grid, 256, frg::ref_laplacian_tma_smem_bytes(), s>>>(a);
+    else
+        frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, frg::ref_laplacian_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
     frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
@@ -501,6 +625,8 @@ frg::SobIterArgs sob_args(fr_handle* h, int iter) {
     a.trace = h->trace;
     a.energy = h->sob_energy;
     a.counter = h->counter;
+    a.tmaps = h->tmaps;
+    a.err = h->dev_err;
     return a;
 }
 
@@ -508,7 +634,8 @@ int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev
     if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
     const frg::SobIterArgs a = sob_args(h, iter);
     const int grids[3] = {h->ts[R_SG].grid, h->ts[R_SS].grid, h->ts[R_SB].grid};
-    cudaError_t e = frg::launch_sob_iter(a, grids, s, ev);
+    const int variants[2] = {h->ts[R_SG].shape.variant, h->ts[R_SS].shape.variant};
+    cudaError_t e = frg::launch_sob_iter(a, grids, variants, s, ev);
     if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "sobolev launch failed: %s", cudaGetErrorString(e));
     return FR_OK;
 }
@@ -676,7 +803,7 @@ int run_registration(fr_handle* h, cudaStream_t s) {
 std::string size_class(const fr_handle* h) {
     std::ostringstream k;
     k << h->P.solver << '/' << h->device << '/' << h->num_sms << '/'
-      << (h->P.solver == FR_SOLVER_SOBOLEV ? h->P.smooth_width : 0);
+      << (h->P.solver == FR_SOLVER_SOBOLEV ? h->P.smooth_width : 0) << '/' << h->P.staging;
     std::vector<std::array<int, 3>> d = h->dims;
     std::sort(d.begin(), d.end());
     for (const auto& x : d) k << '/' << x[0] << 'x' << x[1] << 'x' << x[2];
@@ -700,7 +827,8 @@ int launch_role(fr_handle* h, int r, int iter, float t, cudaStream_t s) {
         sa.max_update_norm = -INFINITY;
         args[0] = &sa;
     }
-    FR_CUDA(h, cudaLaunchKernel(role_fn(h, r), dim3(h->ts[r].grid), dim3(256), args, role_smem(r), s));
+    const int v = h->ts[r].shape.variant;
+    FR_CUDA(h, cudaLaunchKernel(role_fn(h, r, v), dim3(h->ts[r].grid), dim3(256), args, role_smem(r, v), s));
     return FR_OK;
 }
 
@@ -741,14 +869,16 @@ int autotune(fr_handle* h, cudaStream_t s) {
     Shapes best = default_shapes(h);
     int rc = FR_OK;
     for (int r : active_roles(h)) {
-        const int occ = h->ts[r].occ;
-        std::vector<int> bps = {occ};
-        if (occ > 1) bps.push_back(occ - 1);
-        if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
-        bps.push_back(-1);  // one block per tile
         std::vector<Shape> cand;
-        for (int depth : {1, 2, 4, 8, 12, 16, 24, 32, 48})
-            for (int b : bps) cand.push_back(Shape{depth, b});
+        for (int v : allowed_variants(h, r)) {
+            const int occ = h->ts[r].occ[v];
+            std::vector<int> bps = {occ};
+            if (occ > 1) bps.push_back(occ - 1);
+            if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
+            bps.push_back(-1);  // one block per tile
+            for (int depth : {1, 2, 4, 8, 12, 16, 24, 32, 48})
+                for (int b : bps) cand.push_back(Shape{depth, b, v});
+        }
         // two passes over the candidates, each candidate's faster time kept (less noise)
         std::vector<float> best_of(cand.size(), 1e30f);
         for (int pass = 0; pass < 2 && rc == FR_OK; ++pass) {
@@ -783,6 +913,8 @@ int autotune(fr_handle* h, cudaStream_t s) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc != FR_OK) return rc;
+    rc = check_device_error(h);
     if (rc != FR_OK) return rc;
     h->graph_valid = false;
     h->tuned = true;
@@ -829,6 +961,7 @@ int begin(fr_handle* h, const fr_pair* pairs, int n, cudaStream_t s) {
         if (rc != FR_OK) return rc;
     }
     FR_CUDA(h, cudaMemsetAsync(h->stop, 0, sizeof(int) * n, s));
+    FR_CUDA(h, cudaMemsetAsync(h->dev_err, 0, sizeof(unsigned int), s));
     FR_CUDA(h, cudaMemsetAsync(h->keys, 0, sizeof(unsigned long long) * n, s));
     FR_CUDA(h, cudaMemsetAsync(h->trace, 0, sizeof(unsigned long long) * n * (size_t)h->trace_cap, s));
     if (h->sob_energy)
@@ -863,6 +996,10 @@ int host_stats(fr_handle* h) {
     std::vector<long long> folds(n);
     std::vector<unsigned long long> dice((size_t)n * (2 * 256 + 1));
     std::vector<unsigned long long> trace((size_t)n * h->trace_cap);
+    {
+        int rc = check_device_error(h);
+        if (rc != FR_OK) return rc;
+    }
     FR_CUDA(h, cudaMemcpy(stop.data(), h->stop, sizeof(int) * n, cudaMemcpyDeviceToHost));
     FR_CUDA(h, cudaMemcpy(energy.data(), h->pair_energy, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost));
     FR_CUDA(h, cudaMemcpy(folds.data(), h->pair_folds, sizeof(long long) * n, cudaMemcpyDeviceToHost));
@@ -946,6 +1083,7 @@ int set_key(fr_params* p, const std::string& key, const std::string& val, std::s
     else if (key == "STEP") ok = as_float(&p->step);
     else if (key == "KEEP_STATE") ok = as_int(&p->keep_state);
     else if (key == "AUTOTUNE") ok = as_int(&p->autotune);
+    else if (key == "STAGING") ok = as_int(&p->staging);
     else {
         *why = "unrecognised option '" + key + "'";
         return FR_ERR_PARSE;
@@ -1022,6 +1160,7 @@ int fr_params_default(fr_params* p) {
     p->step = 0.5f;
     p->keep_state = 0;
     p->autotune = 1;
+    p->staging = 0;
     return FR_OK;
 }
 
@@ -1302,6 +1441,8 @@ int fr_time_kernels(fr_handle* h, int iters, float* ms, int* n_kernels, void* st
     for (int k = 0; k <= nk; ++k)
         if (ev[k]) cudaEventDestroy(ev[k]);
     if (rc != FR_OK) return rc;
+    rc = check_device_error(h);
+    if (rc != FR_OK) return rc;
     for (int k = 0; k < nk; ++k) ms[k] = (float)(acc[k] / iters);
     if (n_kernels) *n_kernels = nk;
     h->stats_ready = false;
@@ -1401,6 +1542,13 @@ int fr_tile_shape(const fr_handle* h, int k, int* depth, int* blocks_per_sm) {
     const TileSet& t = h->ts[active_roles(h)[k]];
     *depth = t.shape.depth;
     *blocks_per_sm = t.shape.bps;
+    return FR_OK;
+}
+
+int fr_tile_staging(const fr_handle* h, int k, int* tma) {
+    if (!h || !tma || k < 0 || k > 2) return FR_ERR_INVALID_ARG;
+    if (!h->block) return FR_ERR_STATE;
+    *tma = h->ts[active_roles(h)[k]].shape.variant;
     return FR_OK;
 }
 

@@ -3,11 +3,23 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fr_common.cuh"
 
 namespace frg {
+
+// Tensor maps of one pair, in this order, for the kernels that stage through TMA (boxes
+// are part of a map, so each kernel that stages a field has its own map of it).
+enum TmapIndex {
+    TM_LAP_PSI = 0,  // psi, 4-D (x, y, z, component), box 40 x 10 x 1 x 3 (Laplacian)
+    TM_LAP_T,        // T, 3-D, box 32 x 8 x 1 (Laplacian; the sobolev gradient uses both,
+                     // phi living where psi does)
+    TM_SOB_G,        // the sobolev gradient g, 4-D, box (32 + 2 HX) x (8 + 2 R) x 1 x 3 for the
+                     // smoothing radius R (HX = R rounded up to 4)
+    TM_COUNT
+};
 
 // Arguments of one reference-mode iteration (all three launches take the same block).
 struct RefIterArgs {
@@ -41,10 +53,14 @@ struct RefIterArgs {
     unsigned long long* keys;  // per pair: max-norm key of the running iteration
     unsigned long long* trace; // [max_iter][npairs] max-norm keys
     unsigned int* counter;     // last-block ticket of pass B
+    const CUtensorMap* tmaps;  // [npairs][TM_COUNT] tensor maps of the TMA-staged kernels
+    unsigned int* err;         // device error word (kErrTmaTimeout: a staging wait gave up)
 };
 
 size_t ref_laplacian_smem_bytes();  // dynamic shared memory of ref_laplacian_kernel
 __global__ void ref_laplacian_kernel(RefIterArgs a);
+size_t ref_laplacian_tma_smem_bytes();  // dynamic shared memory of ref_laplacian_tma_kernel
+__global__ void ref_laplacian_tma_kernel(RefIterArgs a);
 size_t ref_pass_a_smem_bytes();  // dynamic shared memory of ref_pass_a_kernel
 __global__ void ref_pass_a_kernel(RefIterArgs a);
 __global__ void ref_pass_b_kernel(RefIterArgs a);

@@ -16,6 +16,7 @@
 // at the voxel it writes).  Boundary voxels are never written, as in the reference.
 #include "fr_common.cuh"
 #include "fr_kernels.h"
+#include "fr_tma.cuh"
 
 namespace frg {
 
@@ -166,6 +167,246 @@ __global__ void __launch_bounds__(256) ref_laplacian_kernel(RefIterArgs a) {
     }
 }
 
+// ----------------------------------------------------------------------------------
+// The same Laplacian with TMA staging.  Per slice, one thread issues two tensor copies
+// into the slot's shared memory -- psi's box of 40 columns x 10 rows x 3 components (the
+// tile plus a 1-voxel halo, x0 - 4 .. x0 + 35, y0 - 1 .. y0 + 8; out-of-volume parts read
+// as zero and are never used) and T's 32 x 8 box -- completing on the slot's mbarrier; no
+// other thread computes an address or issues a copy.  A six-slot ring keeps three slices
+// ahead of the one computed (slices z - 1, z, z + 1 are read), and one block barrier per
+// slice frees the slot of slice z - 2 for the next copy.  Every wait is bounded (about a
+// second); a block that gives up sets the device error word, waits (bounded) for its own
+// copies in flight and returns.
+// ----------------------------------------------------------------------------------
+namespace {
+constexpr int kTLAhead = 3;
+constexpr int kTLS = 3 + kTLAhead;                      // ring slots
+constexpr int kTQW = 40, kTQR = 10, kTQPlane = kTQW * kTQR;  // psi box: row, rows, plane (floats)
+constexpr int kTTOff = 1216;                            // T box offset in a slot (floats, 128-byte aligned)
+constexpr int kTSlot = kTTOff + kTileX * kTileY;        // slot stride: 1472 floats = 5888 bytes
+constexpr unsigned kTLBytes = sizeof(float) * (3 * kTQPlane + kTileX * kTileY);  // copied per slice
+static_assert(3 * kTQPlane <= kTTOff && (kTTOff * 4) % 128 == 0 && (kTSlot * 4) % 128 == 0, "slot layout");
+}  // namespace
+
+size_t ref_laplacian_tma_smem_bytes() { return 128 + sizeof(float) * kTLS * kTSlot + sizeof(uint64_t) * kTLS; }
+
+__global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
+    extern __shared__ __align__(128) unsigned char lap_raw[];
+    float* ring = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(lap_raw) + 127) & ~uintptr_t(127));
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kTLS * kTSlot);
+    typedef SliceRing<kTLS> Ring;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    if (tid == 0) {
+        for (int k = 0; k < kTLS; ++k) mbar_init(full + k, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned nbase = 0;    // slices this block has staged before the current tile
+    unsigned issued = 0;   // slices issued so far (thread 0's count)
+    bool failed = false;
+    for (int t = blockIdx.x; t < a.ntiles_l && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_l[t];
+        if (a.stop[tl.x]) continue;  // uniform over the block
+        const Pair P = a.pairs[tl.x];
+        const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XYp = P.Xp * P.Y;
+        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + a.depth_l, Z - 1);
+        if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
+        const CUtensorMap* mpsi = a.tmaps + (long long)tl.x * TM_COUNT + TM_LAP_PSI;
+        const CUtensorMap* mT = a.tmaps + (long long)tl.x * TM_COUNT + TM_LAP_T;
+        float4* LT = a.LT + P.off;
+        const int x = tl.y + tx, y = tl.z + ty;
+        const bool active = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
+        const int nsl = zs1 - zs0 + 2;  // slices zs0 - 1 .. zs1
+        auto issue = [&](int j) {       // slice zs0 - 1 + j of the tile (thread 0)
+            const unsigned n = nbase + (unsigned)j;
+            float* dst = ring + Ring::slot(n) * kTSlot;
+            uint64_t* bar = full + Ring::slot(n);
+            mbar_arrive_expect_tx(bar, kTLBytes);
+            tma_load_4d(dst, mpsi, tl.y - 4, tl.z - 1, zs0 - 1 + j, 0, bar);
+            tma_load_3d(dst + kTTOff, mT, tl.y, tl.z, zs0 - 1 + j, bar);
+            ++issued;
+        };
+        __syncthreads();  // the previous tile is done with the ring
+        if (tid == 0) {
+            tma_prefetch_map(mpsi);
+            tma_prefetch_map(mT);
+            for (int j = 0; j < min(nsl, kTLS); ++j) issue(j);
+        }
+        const int c0 = (ty + 1) * kTQW + tx + 4;
+        for (int j0 = 0; j0 + 2 < nsl; ++j0) {
+            // slices j0, j0 + 1 and j0 + 2 of the tile are read; j0 + 2 is the newest
+            bool ok = true;
+            for (int j = (j0 == 0 ? 0 : j0 + 2); j <= j0 + 2; ++j)
+                ok = ok && mbar_wait_bounded(full + Ring::slot(nbase + j), Ring::parity(nbase + j));
+            // every thread is past step j0 - 1 (the slot of slice j0 - 1 is free), and the
+            // block agrees on whether any wait gave up
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0 && j0 >= 1 && j0 - 1 + kTLS < nsl) issue(j0 - 1 + kTLS);
+            if (active) {
+                const int z = zs0 + j0;
+                const float* qm = ring + Ring::slot(nbase + j0) * kTSlot + c0;
+                const float* q0 = ring + Ring::slot(nbase + j0 + 1) * kTSlot;
+                const float* qp = ring + Ring::slot(nbase + j0 + 2) * kTSlot + c0;
+                float l[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float* q = q0 + c0 + c * kTQPlane;
+                    float s = -6.f * q[0];
+                    s = s + q[1];
+                    s = s + q[-1];
+                    s = s + q[kTQW];
+                    s = s + q[-kTQW];
+                    s = s + qp[c * kTQPlane];
+                    s = s + qm[c * kTQPlane];
+                    l[c] = -1.f * s;
+                }
+                const float tv = q0[kTTOff + ty * kTileX + tx];
+                LT[x + Xp * y + XYp * z] = make_float4(l[0], l[1], l[2], tv);
+            }
+        }
+        nbase += (unsigned)nsl;
+    }
+    if (failed && tid == 0) {
+        // the copies this block issued and nobody waited for: wait for them (bounded)
+        // before the block's shared memory goes away, then report
+        for (unsigned n = (issued > (unsigned)kTLS ? issued - kTLS : 0u); n < issued; ++n)
+            mbar_wait_bounded(full + Ring::slot(n), Ring::parity(n));
+        atomicOr(a.err, kErrTmaTimeout);
+    }
+}
+
+// One voxel of pass A (i = x + Xp (y + Y z), an interior voxel).  vb[k]: this thread's
+// column in the staged slice z - 2 + k of v (component c at + c VC); qb[k]: in the staged
+// slice z - 1 + k of psi_inv (component c at + c QC), rho (at + QR) and S (at + QS); RW is
+// the staged row length.  The arithmetic is the reference's, operation for operation.
+template <int VC, int QC, int QR, int QS, int RW>
+__device__ __forceinline__ void pass_a_voxel(const RefIterArgs& a, const Pair& P, int X, int Y, int Z, int N, int Xp,
+                                             int XYp, int y, int z, int i, bool dv_xy, const float* const vb[5],
+                                             const float* const qb[3], const float4* __restrict__ LT,
+                                             const float* __restrict__ Tg, const float* __restrict__ Sg,
+                                             const float* __restrict__ Rg, const float* __restrict__ const* Vg,
+                                             float* rho_n,
+                                             float* const* Vn, float* const* Qn) {
+    auto V = [&](int k, int c) { return vb[k] + c * VC; };
+    auto Q = [&](int k, int c) { return qb[k] + (c < 3 ? c * QC : (c == 3 ? QR : QS)); };
+    // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
+    const float q[3] = {Q(1, 0)[0], Q(1, 1)[0], Q(1, 2)[0]};
+    const Cell32 cl = locate32(X, Y, Z, Xp, q[0], q[1], q[2]);
+    const float4 lt = tri_unchecked32_f4(LT, Xp, XYp, N, cl);
+    // psi_inv is smooth: the cell of slice z + 1 is about this one plus a slice, so
+    // the rows it adds (two slices above the floor corner) are fetched into L2 now
+    prefetch_l2(LT + min(cl.base + 2 * XYp, N - 1));
+    prefetch_l2(LT + min(cl.base + 2 * XYp + Xp, N - 1));
+    const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
+    const float Lq[3] = {lt.x, lt.y, lt.z};
+
+    // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
+    float M[3][3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        M[r][0] = (Q(1, r)[1] - Q(1, r)[-1]) * 0.5f;
+        M[r][1] = (Q(1, r)[RW] - Q(1, r)[-RW]) * 0.5f;
+        M[r][2] = (Q(2, r)[0] - Q(0, r)[0]) * 0.5f;
+    }
+    const float det = det_ref(M);
+
+    // central-difference gradient of S and the potential gradient
+    // rho and S are read through L1 (their 7-point stencils stay in cache)
+    const float Si = Q(1, 4)[0];
+    if (z + 3 < Z) {  // the S and rho slice this column reads three steps on
+        prefetch_l2(Sg + i + 3 * XYp);
+        prefetch_l2(Rg + i + 3 * XYp);
+    }
+    const float gs[3] = {(Q(1, 4)[1] - Q(1, 4)[-1]) * 0.5f,
+                         (Q(1, 4)[RW] - Q(1, 4)[-RW]) * 0.5f,
+                         (Q(2, 4)[0] - Q(0, 4)[0]) * 0.5f};
+    const float diff = Si - Tq;
+    float gU[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (P.w_reg * Lq[c])) * det;
+
+    // velocity and its 6 neighbours (vb[2] is slice z)
+    float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        vc[c] = V(2, c)[0];
+        vxm[c] = V(2, c)[-1];
+        vxp[c] = V(2, c)[1];
+        vym[c] = V(2, c)[-RW];
+        vyp[c] = V(2, c)[RW];
+        vzm[c] = V(1, c)[0];
+        vzp[c] = V(3, c)[0];
+    }
+    const float vx = vc[0], vy = vc[1], vz = vc[2];
+
+    // divergence of rho*v (upwind) and the density update
+    const float* rb = Q(1, 3);
+    const float p = rb[0];
+    const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * rb[1];
+    const float t12 = (vxm[0] > 0.f) ? vxm[0] * rb[-1] : vxm[0] * p;
+    const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * rb[RW];
+    const float t22 = (vym[1] > 0.f) ? vym[1] * rb[-RW] : vym[1] * p;
+    const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * Q(2, 3)[0];
+    const float t32 = (vzm[2] > 0.f) ? vzm[2] * Q(0, 3)[0] : vzm[2] * p;
+    const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
+    const float rho_new = p + a.alpha * div;
+    rho_n[i] = rho_new;
+
+    // (Dv)v: entropy scheme on the diagonal, upwind off the diagonal
+    const float ax1 = entropy_flux(vx, vxp[0]);
+    const float ax2 = (vy > 0.f) ? vy * (vx - vym[0]) : vy * (vyp[0] - vx);
+    const float ax3 = (vz > 0.f) ? vz * (vx - vzm[0]) : vz * (vzp[0] - vx);
+    const float ay1 = (vx > 0.f) ? vx * (vy - vxm[1]) : vx * (vxp[1] - vy);
+    const float ay2 = entropy_flux(vy, vyp[1]);
+    const float ay3 = (vz > 0.f) ? vz * (vy - vzm[1]) : vz * (vzp[1] - vy);
+    const float az1 = (vx > 0.f) ? vx * (vz - vxm[2]) : vx * (vxp[2] - vz);
+    const float az2 = (vy > 0.f) ? vy * (vz - vym[2]) : vy * (vyp[2] - vz);
+    const float az3 = entropy_flux(vz, vzp[2]);
+    const float dvv[3] = {(0.5f * ax1 + ax2) + ax3, (ay1 + 0.5f * ay2) + ay3,
+                          (az1 + az2) + 0.5f * az3};
+
+    // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
+    // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
+    // reference does; y+2 at y = Y-2 reads index i + 2 rows (voxel (x, 0, z+1))
+    // from global memory, as the reference's unchecked read does
+    float dv[3] = {0.f, 0.f, 0.f};
+    if (dv_xy && z >= 2 && z <= Z - 3) {
+        const bool y_edge = y + 2 > Y - 1;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float xx = (vx < 0.f) ? (V(2, c)[2] - 2.f * vxp[c]) + vc[c]
+                                        : (vc[c] - 2.f * vxm[c]) + V(2, c)[-2];
+            const float vyp2 = y_edge ? __ldg(Vg[c] + i + 2 * Xp) : V(2, c)[2 * RW];
+            const float yy = (vy < 0.f) ? (vyp2 - 2.f * vym[c]) + vc[c]
+                                        : (vc[c] - 2.f * vym[c]) + V(2, c)[-2 * RW];
+            const float zz = (vz < 0.f) ? (V(4, c)[0] - 2.f * vzm[c]) + vc[c]
+                                        : (vc[c] - 2.f * vzm[c]) + V(0, c)[0];
+            dv[c] = -1.f * ((xx + yy) + zz);
+        }
+    }
+
+    // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
+    const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);
+    float vn[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float friction = a.f1 * vc[c];
+        const float diffusion = a.tau * dv[c];
+        const float potential = qd * gU[c];
+        const float acc = ((friction + dvv[c]) - diffusion) + potential;
+        vn[c] = vc[c] - a.alpha * acc;
+        Vn[c][i] = vn[c];
+    }
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        const float jv = ((M[r][0] * vn[0]) + (M[r][1] * vn[1])) + (M[r][2] * vn[2]);
+        Qn[r][i] = q[r] - a.alpha * jv;
+    }
+}
+
 __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
     extern __shared__ __align__(16) float smem[];
     PassASmem sm;
@@ -243,137 +484,23 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
             cp_async_commit();
             if (active) {
                 const int i = x + Xp * y + XYp * z;
-                // per-slice base pointers into the rings (immediate offsets below)
-                const float* vb[5][3];
+                // per-slice base pointers into the rings (immediate offsets from them)
+                const float* vb[5];
 #pragma unroll
                 for (int k = 0; k < 5; ++k) {
                     int sl = sv + k;
                     sl = sl >= kVS ? sl - kVS : sl;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) vb[k][c] = sm.v + (c * kVS + sl) * kVPlane + vc0;
+                    vb[k] = sm.v + sl * kVPlane + vc0;
                 }
-                const float* qb[3][kQC];
+                const float* qb[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     int sl = sq + k;
                     sl = sl >= kQS ? sl - kQS : sl;
-#pragma unroll
-                    for (int c = 0; c < kQC; ++c) qb[k][c] = sm.q + (c * kQS + sl) * kQPlane + qc0;
+                    qb[k] = sm.q + sl * kQPlane + qc0;
                 }
-
-                // T o psi_inv and L o psi_inv, gathered at psi_inv(x)
-                const float q[3] = {qb[1][0][0], qb[1][1][0], qb[1][2][0]};
-                const Cell32 cl = locate32(X, Y, Z, Xp, q[0], q[1], q[2]);
-                const float4 lt = tri_unchecked32_f4(LT, Xp, XYp, N, cl);
-                // psi_inv is smooth: the cell of slice z + 1 is about this one plus a slice, so
-                // the rows it adds (two slices above the floor corner) are fetched into L2 now
-                prefetch_l2(LT + min(cl.base + 2 * XYp, N - 1));
-                prefetch_l2(LT + min(cl.base + 2 * XYp + Xp, N - 1));
-                const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
-                const float Lq[3] = {lt.x, lt.y, lt.z};
-
-                // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
-                float M[3][3];
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    M[r][0] = (qb[1][r][1] - qb[1][r][-1]) * 0.5f;
-                    M[r][1] = (qb[1][r][kQW] - qb[1][r][-kQW]) * 0.5f;
-                    M[r][2] = (qb[2][r][0] - qb[0][r][0]) * 0.5f;
-                }
-                const float det = det_ref(M);
-
-                // central-difference gradient of S and the potential gradient
-                // rho and S are read through L1 (their 7-point stencils stay in cache)
-                const float Si = qb[1][4][0];
-                if (z + 3 < Z) {  // the S and rho slice this column reads three steps on
-                    prefetch_l2(Sg + i + 3 * XYp);
-                    prefetch_l2(Rg + i + 3 * XYp);
-                }
-                const float gs[3] = {(qb[1][4][1] - qb[1][4][-1]) * 0.5f,
-                                     (qb[1][4][kQW] - qb[1][4][-kQW]) * 0.5f,
-                                     (qb[2][4][0] - qb[0][4][0]) * 0.5f};
-                const float diff = Si - Tq;
-                float gU[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (P.w_reg * Lq[c])) * det;
-
-                // velocity and its 6 neighbours (vb[2] is slice z)
-                float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    vc[c] = vb[2][c][0];
-                    vxm[c] = vb[2][c][-1];
-                    vxp[c] = vb[2][c][1];
-                    vym[c] = vb[2][c][-kVW];
-                    vyp[c] = vb[2][c][kVW];
-                    vzm[c] = vb[1][c][0];
-                    vzp[c] = vb[3][c][0];
-                }
-                const float vx = vc[0], vy = vc[1], vz = vc[2];
-
-                // divergence of rho*v (upwind) and the density update
-                const float* rb = qb[1][3];
-                const float p = rb[0];
-                const float t11 = (vx > 0.f) ? (-vx) * p : (-vx) * rb[1];
-                const float t12 = (vxm[0] > 0.f) ? vxm[0] * rb[-1] : vxm[0] * p;
-                const float t21 = (vy > 0.f) ? (-vy) * p : (-vy) * rb[kQW];
-                const float t22 = (vym[1] > 0.f) ? vym[1] * rb[-kQW] : vym[1] * p;
-                const float t31 = (vz > 0.f) ? (-vz) * p : (-vz) * qb[2][3][0];
-                const float t32 = (vzm[2] > 0.f) ? vzm[2] * qb[0][3][0] : vzm[2] * p;
-                const float div = ((((t11 + t12) + t21) + t22) + t31) + t32;
-                const float rho_new = p + a.alpha * div;
-                rho_n[i] = rho_new;
-
-                // (Dv)v: entropy scheme on the diagonal, upwind off the diagonal
-                const float ax1 = entropy_flux(vx, vxp[0]);
-                const float ax2 = (vy > 0.f) ? vy * (vx - vym[0]) : vy * (vyp[0] - vx);
-                const float ax3 = (vz > 0.f) ? vz * (vx - vzm[0]) : vz * (vzp[0] - vx);
-                const float ay1 = (vx > 0.f) ? vx * (vy - vxm[1]) : vx * (vxp[1] - vy);
-                const float ay2 = entropy_flux(vy, vyp[1]);
-                const float ay3 = (vz > 0.f) ? vz * (vy - vzm[1]) : vz * (vzp[1] - vy);
-                const float az1 = (vx > 0.f) ? vx * (vz - vxm[2]) : vx * (vxp[2] - vz);
-                const float az2 = (vy > 0.f) ? vy * (vz - vym[2]) : vy * (vyp[2] - vz);
-                const float az3 = entropy_flux(vz, vzp[2]);
-                const float dvv[3] = {(0.5f * ax1 + ax2) + ax3, (ay1 + 0.5f * ay2) + ay3,
-                                      (az1 + az2) + 0.5f * az3};
-
-                // negated upwind second differences of v (x in [2,X-3], y in [2,Y-2],
-                // z in [2,Z-3]); the y and z forward branches read (+2, -1, 0) as the
-                // reference does; y+2 at y = Y-2 reads index i + 2 rows (voxel (x, 0, z+1))
-                // from global memory, as the reference's unchecked read does
-                float dv[3] = {0.f, 0.f, 0.f};
-                if (dv_xy && z >= 2 && z <= Z - 3) {
-                    const bool y_edge = y + 2 > Y - 1;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        const float xx = (vx < 0.f) ? (vb[2][c][2] - 2.f * vxp[c]) + vc[c]
-                                                    : (vc[c] - 2.f * vxm[c]) + vb[2][c][-2];
-                        const float vyp2 = y_edge ? __ldg(Vg[c] + i + 2 * Xp) : vb[2][c][2 * kVW];
-                        const float yy = (vy < 0.f) ? (vyp2 - 2.f * vym[c]) + vc[c]
-                                                    : (vc[c] - 2.f * vym[c]) + vb[2][c][-2 * kVW];
-                        const float zz = (vz < 0.f) ? (vb[4][c][0] - 2.f * vzm[c]) + vc[c]
-                                                    : (vc[c] - 2.f * vzm[c]) + vb[0][c][0];
-                        dv[c] = -1.f * ((xx + yy) + zz);
-                    }
-                }
-
-                // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
-                const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);
-                float vn[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float friction = a.f1 * vc[c];
-                    const float diffusion = a.tau * dv[c];
-                    const float potential = qd * gU[c];
-                    const float acc = ((friction + dvv[c]) - diffusion) + potential;
-                    vn[c] = vc[c] - a.alpha * acc;
-                    Vn[c][i] = vn[c];
-                }
-#pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    const float jv = ((M[r][0] * vn[0]) + (M[r][1] * vn[1])) + (M[r][2] * vn[2]);
-                    Qn[r][i] = q[r] - a.alpha * jv;
-                }
+                pass_a_voxel<kVS * kVPlane, kQS * kQPlane, 3 * kQS * kQPlane, 4 * kQS * kQPlane, kVW>(
+                    a, P, X, Y, Z, N, Xp, XYp, y, z, i, dv_xy, vb, qb, LT, Tg, Sg, Rg, Vg, rho_n, Vn, Qn);
             }
             sv = sv + 1 == kVS ? 0 : sv + 1;
             sq = sq + 1 == kQS ? 0 : sq + 1;

@@ -7,7 +7,9 @@
 #include <cmath>
 
 #include "fr_common.cuh"
+#include "fr_kernels.h"
 #include "fr_sob.h"
+#include "fr_tma.cuh"
 
 namespace frg {
 
@@ -173,6 +175,133 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
     }
 }
 
+// The same gradient with TMA staging: per slice one thread copies phi's box (40 columns
+// x 10 rows x 3 components: the tile and a 1-voxel halo; out-of-volume parts read as zero
+// and are masked by the grid-neighbour tests) and T's 32 x 8 box with two tensor copies
+// into a six-slot ring, completing on the slot's mbarrier; three slices are in flight
+// ahead of the one computed.  Waits are bounded as in ref_laplacian_tma_kernel.
+namespace {
+constexpr int kGBAhead = 3;
+constexpr int kGBS = 3 + kGBAhead;
+constexpr int kGBW = 40, kGBPlane = kGBW * 10;  // phi box row and plane (floats)
+constexpr int kGBTOff = 1216;                   // T box offset in a slot (floats, 128-byte aligned)
+constexpr int kGBSlot = kGBTOff + kTileX * kTileY;
+constexpr unsigned kGBBytes = sizeof(float) * (3 * kGBPlane + kTileX * kTileY);
+static_assert(3 * kGBPlane <= kGBTOff && (kGBSlot * 4) % 128 == 0, "slot layout");
+}  // namespace
+
+size_t sob_grad_tma_smem_bytes() { return 128 + sizeof(float) * kGBS * kGBSlot + sizeof(uint64_t) * kGBS; }
+
+__global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
+    extern __shared__ __align__(128) unsigned char grad_raw[];
+    float* ring = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(grad_raw) + 127) & ~uintptr_t(127));
+    uint64_t* full = reinterpret_cast<uint64_t*>(ring + kGBS * kGBSlot);
+    __shared__ double red[32];
+    typedef SliceRing<kGBS> Ring;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    if (tid == 0) {
+        for (int k = 0; k < kGBS; ++k) mbar_init(full + k, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned nbase = 0, issued = 0;
+    bool failed = false;
+    for (int t = blockIdx.x; t < a.ntiles_g && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_g[t];
+        if (a.stop[tl.x]) continue;  // uniform over the block
+        const Pair P = a.pairs[tl.x];
+        const int Y = P.Y, Z = P.Z, Xp = P.Xp, XYp = P.Xp * P.Y;
+        const long long NT = a.NT;
+        const float* __restrict__ S = a.S + P.off;
+        float* G[3] = {a.g + P.off, a.g + NT + P.off, a.g + 2 * NT + P.off};
+        const CUtensorMap* mphi = a.tmaps + (long long)tl.x * TM_COUNT + TM_LAP_PSI;
+        const CUtensorMap* mT = a.tmaps + (long long)tl.x * TM_COUNT + TM_LAP_T;
+        const int x = tl.y + tx, y = tl.z + ty;
+        const bool inside = x < P.X && y < Y;
+        const int z0 = tl.w, z1 = min(tl.w + a.depth_g, Z);
+        const int nsl = z1 - z0 + 2;  // slices z0 - 1 .. z1 (outside the volume: zeros, unused)
+        auto issue = [&](int j) {
+            const unsigned n = nbase + (unsigned)j;
+            float* dst = ring + Ring::slot(n) * kGBSlot;
+            uint64_t* bar = full + Ring::slot(n);
+            mbar_arrive_expect_tx(bar, kGBBytes);
+            tma_load_4d(dst, mphi, tl.y - 4, tl.z - 1, z0 - 1 + j, 0, bar);
+            tma_load_3d(dst + kGBTOff, mT, tl.y, tl.z, z0 - 1 + j, bar);
+            ++issued;
+        };
+        double e = 0.0;
+        __syncthreads();  // the previous tile is done with the ring
+        if (tid == 0) {
+            tma_prefetch_map(mphi);
+            tma_prefetch_map(mT);
+            for (int j = 0; j < min(nsl, kGBS); ++j) issue(j);
+        }
+        const int c0 = (ty + 1) * kGBW + tx + 4;
+        for (int j0 = 0; j0 + 2 < nsl; ++j0) {
+            bool ok = true;
+            for (int j = (j0 == 0 ? 0 : j0 + 2); j <= j0 + 2; ++j)
+                ok = ok && mbar_wait_bounded(full + Ring::slot(nbase + j), Ring::parity(nbase + j));
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0 && j0 >= 1 && j0 - 1 + kGBS < nsl) issue(j0 - 1 + kGBS);
+            if (inside) {
+                const int z = z0 + j0;
+                const int i = x + Xp * y + XYp * z;
+                const float* qm = ring + Ring::slot(nbase + j0) * kGBSlot + c0;
+                const float* q0 = ring + Ring::slot(nbase + j0 + 1) * kGBSlot;
+                const float* qp = ring + Ring::slot(nbase + j0 + 2) * kGBSlot + c0;
+                const SobCell s = sob_locate(P, q0[c0], q0[c0 + kGBPlane], q0[c0 + 2 * kGBPlane]);
+                const int b = (int)s.base;
+                const float f000 = __ldg(S + b), f100 = __ldg(S + b + 1);
+                const float f010 = __ldg(S + b + Xp), f110 = __ldg(S + b + 1 + Xp);
+                const float f001 = __ldg(S + b + XYp), f101 = __ldg(S + b + 1 + XYp);
+                const float f011 = __ldg(S + b + Xp + XYp), f111 = __ldg(S + b + 1 + Xp + XYp);
+                const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
+                const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
+                const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
+                const float W = lerpf_(A1, A0, s.a);
+                const float dWa = s.in_x ? A1 - A0 : 0.f;
+                const float dWb = s.in_y ? lerpf_(e11 - e10, e01 - e00, s.a) : 0.f;
+                const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
+                                                  lerpf_(f011 - f010, f001 - f000, s.b), s.a)
+                                         : 0.f;
+                const float r = W - q0[kGBTOff + ty * kTileX + tx];
+                const bool okn[6] = {x > 0, x < P.X - 1, y > 0, y < Y - 1, z > 0, z < Z - 1};
+                float lap[3];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float* qc = q0 + c0 + c * kGBPlane;
+                    const float pc = qc[0];
+                    const float nb[6] = {qc[-1], qc[1], qc[-kGBW], qc[kGBW], qm[c * kGBPlane], qp[c * kGBPlane]};
+                    float acc = 0.f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        if (!okn[k]) continue;
+                        const float delta = (k / 2 == c) ? ((k & 1) ? 1.f : -1.f) : 0.f;
+                        acc = acc + ((pc - nb[k]) + delta);
+                    }
+                    lap[c] = acc;
+                }
+                G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
+                G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
+                G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
+                e += (double)r * (double)r;
+            }
+        }
+        nbase += (unsigned)nsl;
+        if (failed) break;
+        e = block_sum_f64(e, red);
+        if (threadIdx.x == 0) atomicAdd(a.energy + (long long)(a.iter - 1) * a.npairs + tl.x, 0.5 * e);
+    }
+    if (failed && tid == 0) {
+        for (unsigned n = (issued > (unsigned)kGBS ? issued - kGBS : 0u); n < issued; ++n)
+            mbar_wait_bounded(full + Ring::slot(n), Ring::parity(n));
+        atomicOr(a.err, kErrTmaTimeout);
+    }
+}
+
 // Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
 // fused with the momentum update m = damping * m - step * gs.  A block owns a 32 x 8
 // column tile and marches z.  Each input slice (the tile's rows plus an R halo, clamped
@@ -313,6 +442,148 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
     }
 }
 
+// The same smoothing with TMA staging: each input slice (3 components of the tile's rows
+// plus an R halo and columns x0 - HX .. x0 + 31 + HX) is one tensor copy, issued by one
+// thread NT - 1 slices ahead into a ring of NT buffers and completed on the buffer's
+// mbarrier.  Rows and slices outside the volume realise the replicate boundary: a slice
+// beyond an end is requested at the clamped z, and the x pass reads, for each staged row,
+// the row of the clamped y (inside the box whenever the tile is inside the volume); the
+// zeros that the copy writes outside the volume are never read.  Waits are bounded as in
+// ref_laplacian_tma_kernel.
+template <int R>
+__global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
+    constexpr int HX = (R + 3) / 4 * 4;
+    constexpr int WS = kTileX + 2 * HX;
+    constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
+    constexpr int BOX = 3 * H * WS;                    // floats copied per slice
+    constexpr int BSTRIDE = (BOX + 31) / 32 * 32;      // buffer stride: 128-byte multiple
+    // buffers: as many (up to 4) as keep the block's static shared memory within 48 KB
+    constexpr int NT = 4 * (4 * BSTRIDE + 2 * 3 * H * kTileX) + 32 <= 48 * 1024   ? 4
+                       : 4 * (3 * BSTRIDE + 2 * 3 * H * kTileX) + 24 <= 48 * 1024 ? 3
+                                                                                  : 2;
+    constexpr int RW = (3 * H + kSobTileY - 1) / kSobTileY;
+    __shared__ __align__(128) float G[NT][BSTRIDE];
+    __shared__ float Gx[2][3][H][kTileX];
+    __shared__ __align__(8) uint64_t full[NT];
+    typedef SliceRing<NT> Ring;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    if (tid == 0) {
+        for (int k = 0; k < NT; ++k) mbar_init(full + k, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    unsigned nbase = 0, issued = 0;
+    bool failed = false;
+
+    for (int t = blockIdx.x; t < a.ntiles_s && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_s[t];
+        if (a.stop[tl.x]) continue;  // uniform over the block
+        const Pair P = a.pairs[tl.x];
+        const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XY = P.Xp * P.Y;
+        const long long NTv = a.NT;
+        float* m[3] = {a.m + P.off, a.m + NTv + P.off, a.m + 2 * NTv + P.off};
+        const CUtensorMap* mg = a.tmaps + (long long)tl.x * TM_COUNT + TM_SOB_G;
+        const int x0 = tl.y, y0 = tl.z, zt0 = tl.w, zt1 = min(tl.w + a.depth_s, Z);
+        const int nsl = (zt1 - zt0) + 2 * R;
+        const bool xedge = x0 - R < 0 || x0 + kTileX - 1 + R > X - 1;  // uniform over the block
+        auto issue = [&](int k) {  // staged slice k of the tile (z = zt0 - R + k, clamped)
+            const unsigned n = nbase + (unsigned)k;
+            uint64_t* bar = full + Ring::slot(n);
+            mbar_arrive_expect_tx(bar, sizeof(float) * BOX);
+            tma_load_4d(&G[Ring::slot(n)][0], mg, x0 - HX, y0 - R, min(max(zt0 - R + k, 0), Z - 1), 0, bar);
+            ++issued;
+        };
+        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
+            const float* src = &G[Ring::slot(nbase + (unsigned)k)][0];
+            float* dst = &Gx[k & 1][0][0][0];
+#pragma unroll
+            for (int j = 0; j < RW; ++j) {
+                const int rr = ty + kSobTileY * j;  // row rr of the 3 H staged rows
+                if (rr < 3 * H) {
+                    const int c = rr / H, r = rr - c * H;
+                    const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);  // the clamped row
+                    const float* row = src + (c * H + rs) * WS;
+                    float acc = 0.f;
+                    if (!xedge) {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], row[HX - R + tx + q], acc);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) {
+                            const int xi = min(max(x0 - R + tx + q, 0), X - 1);
+                            acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
+                        }
+                    }
+                    dst[rr * kTileX + tx] = acc;
+                }
+            }
+        };
+        auto wait = [&](int k) {
+            return mbar_wait_bounded(full + Ring::slot(nbase + (unsigned)k), Ring::parity(nbase + (unsigned)k));
+        };
+
+        const int x = x0 + tx, y = y0 + ty, col = x + Xp * y;
+        const bool inside = x < X && y < Y;
+        float mv[3] = {0.f, 0.f, 0.f};
+        if (inside)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) mv[c] = m[c][col + XY * zt0];
+
+        float ring[K][3];
+        __syncthreads();  // the previous tile is done with G and Gx
+        if (tid == 0) {
+            tma_prefetch_map(mg);
+            for (int k = 0; k < min(NT, nsl); ++k) issue(k);
+        }
+        if (__syncthreads_or(!wait(0))) {  // slice 0 has landed
+            failed = true;
+            break;
+        }
+        x_pass(0);
+        for (int k = 0; k < nsl; ++k) {
+            const bool ok = k + 1 < nsl ? wait(k + 1) : true;  // slice k + 1 has landed
+            // every thread is past step k - 1: Gx[k & 1] is complete, slice k's buffer and
+            // Gx[(k + 1) & 1] are no longer read; and the block agrees on the waits
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0 && k + NT < nsl) issue(k + NT);  // into slice k's buffer
+            if (k + 1 < nsl) x_pass(k + 1);
+#pragma unroll
+            for (int q = 0; q < K - 1; ++q)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ring[q][c] = ring[q + 1][c];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float acc = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], Gx[k & 1][c][ty + q][tx], acc);
+                ring[K - 1][c] = acc;
+            }
+            const int zo = zt0 - 2 * R + k;
+            if (k >= 2 * R && inside) {
+                const int i = col + XY * zo;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float acc = 0.f;
+#pragma unroll
+                    for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], ring[q][c], acc);
+                    const float mo = mv[c];
+                    if (zo + 1 < zt1) mv[c] = m[c][i + XY];
+                    m[c][i] = a.damping * mo - a.step * acc;
+                }
+            }
+        }
+        nbase += (unsigned)nsl;
+    }
+    if (failed && tid == 0) {
+        for (unsigned n = (issued > (unsigned)NT ? issued - NT : 0u); n < issued; ++n)
+            mbar_wait_bounded(full + Ring::slot(n), Ring::parity(n));
+        atomicOr(a.err, kErrTmaTimeout);
+    }
+}
+
 __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
     __shared__ unsigned long long red[32];
     __shared__ bool last;
@@ -392,19 +663,17 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
     if (threadIdx.x == 0) *a.counter = 0u;
 }
 
-cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t s, cudaEvent_t* ev) {
+cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, const int* variants, cudaStream_t s,
+                            cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
-    sob_grad_kernel<<<grids[0], 256, sob_grad_smem_bytes(), s>>>(a);
+    if (variants[0])
+        sob_grad_tma_kernel<<<grids[0], 256, sob_grad_tma_smem_bytes(), s>>>(a);
+    else
+        sob_grad_kernel<<<grids[0], 256, sob_grad_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    switch (a.radius) {
-        case 0: sob_smooth3_kernel<0><<<grids[1], 256, 0, s>>>(a); break;
-        case 1: sob_smooth3_kernel<1><<<grids[1], 256, 0, s>>>(a); break;
-        case 2: sob_smooth3_kernel<2><<<grids[1], 256, 0, s>>>(a); break;
-        case 3: sob_smooth3_kernel<3><<<grids[1], 256, 0, s>>>(a); break;
-        case 4: sob_smooth3_kernel<4><<<grids[1], 256, 0, s>>>(a); break;
-        case 5: sob_smooth3_kernel<5><<<grids[1], 256, 0, s>>>(a); break;
-        case 6: sob_smooth3_kernel<6><<<grids[1], 256, 0, s>>>(a); break;
-        default: sob_smooth3_kernel<7><<<grids[1], 256, 0, s>>>(a); break;
+    {
+        void* args[1] = {const_cast<SobIterArgs*>(&a)};
+        cudaLaunchKernel(sob_smooth3_fn(a.radius, variants[1]), dim3(grids[1]), dim3(256), args, 0, s);
     }
     if (ev) cudaEventRecord(ev[2], s);
     sob_pass_b_kernel<<<grids[2], 256, 0, s>>>(a);
@@ -412,7 +681,19 @@ cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t
     return cudaGetLastError();
 }
 
-const void* sob_smooth3_fn(int radius) {
+const void* sob_smooth3_fn(int radius, int variant) {
+    if (variant) {
+        switch (radius) {
+            case 0: return (const void*)sob_smooth3_tma_kernel<0>;
+            case 1: return (const void*)sob_smooth3_tma_kernel<1>;
+            case 2: return (const void*)sob_smooth3_tma_kernel<2>;
+            case 3: return (const void*)sob_smooth3_tma_kernel<3>;
+            case 4: return (const void*)sob_smooth3_tma_kernel<4>;
+            case 5: return (const void*)sob_smooth3_tma_kernel<5>;
+            case 6: return (const void*)sob_smooth3_tma_kernel<6>;
+            default: return (const void*)sob_smooth3_tma_kernel<7>;
+        }
+    }
     switch (radius) {
         case 0: return (const void*)sob_smooth3_kernel<0>;
         case 1: return (const void*)sob_smooth3_kernel<1>;

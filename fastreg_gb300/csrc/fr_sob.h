@@ -14,6 +14,7 @@
 //   phi(x) = phi(x) + m(phi(x))                trilinear gather of the new m
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "fr_common.cuh"
@@ -51,6 +52,8 @@ struct SobIterArgs {
     unsigned long long* trace;
     double* energy;  // [max_iter][npairs] 0.5 * sum (W - T)^2 before the update
     unsigned int* counter;
+    const CUtensorMap* tmaps;  // [npairs][TM_COUNT] tensor maps (fr_kernels.h), TMA-staged variants
+    unsigned int* err;         // device error word (kErrTmaTimeout: a staging wait gave up)
 };
 
 // Gaussian taps exp(-k^2 / (2 sigma^2)), k = -R..R, normalised; computed in double
@@ -59,10 +62,20 @@ void gaussian_taps(float sigma, int width, float* taps);
 
 size_t sob_grad_smem_bytes();  // dynamic shared memory of sob_grad_kernel
 __global__ void sob_grad_kernel(SobIterArgs a);
-const void* sob_smooth3_fn(int radius);  // the smoothing kernel instance for a radius
+size_t sob_grad_tma_smem_bytes();  // dynamic shared memory of sob_grad_tma_kernel
+__global__ void sob_grad_tma_kernel(SobIterArgs a);
+// the smoothing kernel instance for a radius and staging variant (1: TMA)
+const void* sob_smooth3_fn(int radius, int variant = 0);
+// box of the smoothing kernel's staged slice for radius R: x extent, rows
+inline void sob_smooth_box(int R, int* wx, int* rows) {
+    *wx = kTileX + 2 * ((R + 3) / 4 * 4);
+    *rows = kSobTileY + 2 * R;
+}
 __global__ void sob_pass_b_kernel(SobIterArgs a);
 
-// grids: {grad, smooth, pass_b}; with `ev` (4 events) each launch is bracketed
-cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, cudaStream_t s, cudaEvent_t* ev = nullptr);
+// grids: {grad, smooth, pass_b}; variants: staging of {grad, smooth} (1: TMA); with `ev`
+// (4 events) each launch is bracketed
+cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, const int* variants, cudaStream_t s,
+                            cudaEvent_t* ev = nullptr);
 
 }  // namespace frg

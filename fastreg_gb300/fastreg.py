@@ -38,6 +38,7 @@ class Params:
     step: float = 0.5
     keep_state: int = 0
     autotune: int = 1
+    staging: int = 0
 
     @classmethod
     def from_c(cls, c: N.fr_params) -> "Params":
@@ -47,7 +48,7 @@ class Params:
             alpha=c.alpha, p=c.p, C=c.C, reset_iter=c.reset_iter, verbosity=c.verbosity,
             solver="sobolev" if c.solver == N.FR_SOLVER_SOBOLEV else "reference",
             smooth_sigma=c.smooth_sigma, smooth_width=c.smooth_width, damping=c.damping, step=c.step,
-            keep_state=c.keep_state, autotune=c.autotune)
+            keep_state=c.keep_state, autotune=c.autotune, staging=c.staging)
 
     def to_c(self) -> N.fr_params:
         c = N.fr_params()
@@ -71,6 +72,7 @@ class Params:
         c.step = float(self.step)
         c.keep_state = int(self.keep_state)
         c.autotune = int(self.autotune)
+        c.staging = int(self.staging)
         return c
 
     @classmethod
@@ -258,6 +260,16 @@ class FastReg:
             d, b = C.c_int(), C.c_int()
             N.check(self.lib.fr_tile_shape(self.h, k, C.byref(d), C.byref(b)), self.h, "fr_tile_shape")
             out.append((d.value, b.value))
+        return out
+
+    def tile_staging(self):
+        """Per kernel of the active solver, in launch order: "tma" when it stages its
+        operands with tensor copies, "cp.async" otherwise."""
+        out = []
+        for k in range(3):
+            v = C.c_int()
+            N.check(self.lib.fr_tile_staging(self.h, k, C.byref(v)), self.h, "fr_tile_staging")
+            out.append("tma" if v.value else "cp.async")
         return out
 
     # helpers

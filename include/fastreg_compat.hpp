@@ -64,13 +64,14 @@ struct Params {
     float max_update_norm = -1e-10f, tau = 0.2f, rho_0 = 1.f, alpha = 0.004f, w_reg = 0.2f, p = 2.f, C = 0.25f;
 
     // additions of fastreg_gb300 (params.ini keys SOLVER, SMOOTH_SIGMA, SMOOTH_WIDTH, DAMPING, STEP, KEEP_STATE,
-    // AUTOTUNE)
+    // AUTOTUNE, STAGING)
     int solver = FR_SOLVER_REFERENCE;
     float smooth_sigma = 1.5f;
     int smooth_width = 7;
     float damping = 0.9f, step = 0.5f;
     int keep_state = 0;
     int autotune = 1;
+    int staging = 0;
 
     int no_voxels() { return volume_dims[0] * volume_dims[1] * volume_dims[2]; }
     cv::Vec3f voxel_sizes() {
@@ -113,6 +114,7 @@ struct Params {
         c.step = step;
         c.keep_state = keep_state;
         c.autotune = autotune;
+        c.staging = staging;
         return c;
     }
 
@@ -139,6 +141,7 @@ struct Params {
         step = c.step;
         keep_state = c.keep_state;
         autotune = c.autotune;
+        staging = c.staging;
     }
 };
 

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define FR_ABI_VERSION 2
+#define FR_ABI_VERSION 3
 
 /* status codes */
 #define FR_OK 0
@@ -70,6 +70,10 @@ typedef struct fr_params {
     int autotune;          /* AUTOTUNE=1 (default): time a few tile shapes and block counts
                               per kernel on the first registration of a size class and
                               keep the fastest (results do not depend on the shapes) */
+    int staging;           /* STAGING=0 (default): each kernel's staging is the default or
+                              the autotuner's choice; 1: per-thread cp.async only; 2: TMA
+                              tensor copies wherever a kernel has them (results do not
+                              depend on it) */
 } fr_params;
 
 typedef struct fr_handle fr_handle;
@@ -155,6 +159,12 @@ int fr_set_pair_w_reg(fr_handle *h, const float *w_reg, int n);
  * fr_register / fr_begin: slices per tile and blocks per SM (-1: one block per tile),
  * the defaults or the autotuner's choice (AUTOTUNE). */
 int fr_tile_shape(const fr_handle *h, int k, int *depth, int *blocks_per_sm);
+
+/* How kernel k (as in fr_tile_shape) stages its stencil operands after the last
+ * fr_register / fr_begin: *tma = 1 for tensor copies (TMA, cp.async.bulk.tensor), 0 for
+ * per-thread 16-byte cp.async; the default or the autotuner's choice.  No counterpart in
+ * the reference. */
+int fr_tile_staging(const fr_handle *h, int k, int *tma);
 
 /* ---- standalone kernels of the hot path ---- */
 /* apply (vector_fields.cu:81-107): out = img o pos (trilinear), out_lab = lab at the floor

@@ -930,15 +930,21 @@ static void tri_eval_(const fro_dims *d, const real *F, const fro_scell *s, fro_
     if (in[1] && in[2]) t->H[1][2] = t->H[2][1] = H12;
 }
 
-/* out(x) = sum_k w_k in(clamp(x + k)) along axis: transpose, scatter form */
+/* out(x) = sum_k w_k in(clamp(x + k)) along axis: transpose, scatter form.  A
+ * scatter stays on its line along `axis`, so lines are independent: the loop is split
+ * over slices (axis x, y) or rows (axis z), and every line still receives its
+ * contributions in increasing position -- the same sums for any thread count. */
 static void smooth_t_(const fro_dims *d, const real *taps, int Rr, int axis, const real *src, real *dst) {
     const int64_t N = nvox(d);
     const int dim = axis == 0 ? d->X : (axis == 1 ? d->Y : d->Z);
     const int64_t stride = axis == 0 ? 1 : (axis == 1 ? (int64_t)d->X : (int64_t)d->X * d->Y);
     memset(dst, 0, sizeof(real) * 3 * N);
-    for (int z = 0; z < d->Z; ++z)
-        for (int y = 0; y < d->Y; ++y)
+    const int outer = axis == 2 ? d->Y : d->Z, inner = axis == 2 ? d->Z : d->Y;
+#pragma omp parallel for schedule(static)
+    for (int o = 0; o < outer; ++o)
+        for (int n = 0; n < inner; ++n)
             for (int x = 0; x < d->X; ++x) {
+                const int z = axis == 2 ? n : o, y = axis == 2 ? o : n;
                 const int64_t i = lin(d, x, y, z);
                 const int pos = axis == 0 ? x : (axis == 1 ? y : z);
                 for (int k = -Rr; k <= Rr; ++k) {
@@ -1022,11 +1028,16 @@ double FN(sob_loss_grad)(const int *dims, const fro_sobgrad_params *P, const rea
     for (int64_t i = 0; i < N3; ++i) mbar[i] = R(0.2) * mK[i];
     real *pbar_k = (real *)malloc(sizeof(real) * N3);
     real *gbar = (real *)malloc(sizeof(real) * N3);
+    int64_t *cell_base = (int64_t *)malloc(sizeof(int64_t) * N);
+    real *cell_w = (real *)malloc(sizeof(real) * 8 * N);
+    double *lpart = (double *)malloc(sizeof(double) * d.Z);
     double lbar = 0.0;
     for (int k = K - 1; k >= 0; --k) {
         const real *phi = phis + (int64_t)k * N3, *mn = ms + (int64_t)(k + 1) * N3;
-        /* phi_{k+1} = phi_k + m_{k+1}(phi_k) */
+        /* phi_{k+1} = phi_k + m_{k+1}(phi_k): the per-voxel part in parallel (it reads m,
+         * which nothing here writes), then the scatter into mbar in voxel order */
         memcpy(pbar_k, pbar, sizeof(real) * N3);
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < N; ++i) {
             fro_scell s;
             sob_locate_(&d, phi[i], phi[N + i], phi[2 * N + i], &s);
@@ -1035,10 +1046,23 @@ double FN(sob_loss_grad)(const int *dims, const fro_sobgrad_params *P, const rea
                 tri_eval_(&d, mn + c * N, &s, &t, 0);
                 const real pb = pbar[c * N + i];
                 for (int j = 0; j < 3; ++j) pbar_k[j * N + i] += pb * t.d[j];
-                for (int q = 0; q < 8; ++q) mbar[c * N + t.off[q]] += t.w[q] * pb;
+                if (c == 0) {
+                    cell_base[i] = t.off[0];
+                    for (int q = 0; q < 8; ++q) cell_w[8 * i + q] = t.w[q];
+                }
             }
         }
+        {
+            const int64_t X = d.X, XY = (int64_t)d.X * d.Y;
+            const int64_t off[8] = {0, 1, X, 1 + X, XY, 1 + XY, X + XY, 1 + X + XY};
+            for (int64_t i = 0; i < N; ++i)
+                for (int c = 0; c < 3; ++c) {
+                    const real pb = pbar[c * N + i];
+                    for (int q = 0; q < 8; ++q) mbar[c * N + cell_base[i] + off[q]] += cell_w[8 * i + q] * pb;
+                }
+        }
         /* m_{k+1} = damping * m_k - step * gs */
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < N3; ++i) {
             g[i] = -P->step * mbar[i];
             mbar[i] = P->damping * mbar[i];
@@ -1047,14 +1071,17 @@ double FN(sob_loss_grad)(const int *dims, const fro_sobgrad_params *P, const rea
         smooth_t_(&d, taps, Rr, 2, g, tmp);
         smooth_t_(&d, taps, Rr, 1, tmp, g);
         smooth_t_(&d, taps, Rr, 0, g, gbar);
-        /* g = r dW + lambda lap(u) */
-        for (int z = 0; z < d.Z; ++z)
+        /* g = r dW + lambda lap(u): per voxel, in parallel over slices; dJ/dlambda from
+         * per-slice partial sums added in slice order */
+#pragma omp parallel for schedule(static)
+        for (int z = 0; z < d.Z; ++z) {
+            double lz = 0.0;
             for (int y = 0; y < d.Y; ++y)
                 for (int x = 0; x < d.X; ++x) {
                     const int64_t i = lin(&d, x, y, z);
                     real lap[3];
                     lap_u_(&d, phi, x, y, z, lap);
-                    for (int c = 0; c < 3; ++c) lbar += (double)gbar[c * N + i] * (double)lap[c];
+                    for (int c = 0; c < 3; ++c) lz += (double)gbar[c * N + i] * (double)lap[c];
                     /* Laplacian part: graph Laplacian is symmetric */
                     const int64_t X = d.X, XY = (int64_t)d.X * d.Y;
                     const int ok[6] = {x > 0, x < d.X - 1, y > 0, y < d.Y - 1, z > 0, z < d.Z - 1};
@@ -1076,11 +1103,15 @@ double FN(sob_loss_grad)(const int *dims, const fro_sobgrad_params *P, const rea
                         pbar_k[j * N + i] += gd * t.d[j] + r * h;
                     }
                 }
+            lpart[z] = lz;
+        }
+        for (int z = 0; z < d.Z; ++z) lbar += lpart[z];
         memcpy(pbar, pbar_k, sizeof(real) * N3);
     }
     memcpy(grad_v0, mbar, sizeof(real) * N3);
     *grad_lambda = lbar;
     free(phis); free(ms); free(g); free(tmp); free(pbar); free(mbar); free(pbar_k); free(gbar);
+    free(cell_base); free(cell_w); free(lpart);
     return J;
 }
 

@@ -41,7 +41,7 @@ def test_library_loads_and_exports_every_declared_symbol():
         getattr(lib, name)  # resolvable through ctypes
     # everything the ctypes binding wraps is declared
     assert {n for n, _, _ in N.SIGNATURES} <= decl
-    assert lib.fr_abi_version() == 2
+    assert lib.fr_abi_version() == 3
 
 
 REFERENCE_INI = """# IMAGES
@@ -88,6 +88,7 @@ def test_params_ini_variant_keys_and_errors(tmp_path):
     assert abs(P.damping - 0.8) < 1e-7 and P.step == 0.25 and P.keep_state == 1 and P.max_iter == 7
     assert P.autotune == 1  # the default
     assert Params.from_ini_text("AUTOTUNE=0\n").autotune == 0
+    assert P.staging == 0 and Params.from_ini_text("STAGING=2\n").staging == 2
     with pytest.raises(N.FastRegError) as e:
         Params.from_ini_text("NOT_A_KEY=1\n")
     assert e.value.status == N.FR_ERR_PARSE and "NOT_A_KEY" in str(e.value)
@@ -109,7 +110,7 @@ def test_invalid_params_are_rejected_with_status():
     lib = N.load()
     h = C.c_void_p()
     for bad in (dict(no_labels=0), dict(no_labels=300), dict(max_iter=-1), dict(alpha=0.0),
-                dict(solver="sobolev", smooth_width=8), dict(verbosity=5)):
+                dict(solver="sobolev", smooth_width=8), dict(verbosity=5), dict(staging=3)):
         P = Params(**bad)
         c = P.to_c()
         if "solver" in bad:

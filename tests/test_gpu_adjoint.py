@@ -165,3 +165,90 @@ def test_hypergradient_tuned_cohort(cuda):
         assert torch.equal(fr.get_field(N.FR_FIELD_PSI, pair=k), alone.get_field(N.FR_FIELD_PSI)), k
         alone.close()
     fr.close()
+
+
+@pytest.mark.slow
+def test_adjoint_at_128cube_50_iterations(cuda):
+    """The differentiated workload at its stated size: the 128^3 pair (blobs, max
+    displacement 4 voxels), 50 unrolled sobolev iterations, checkpoints every 10,
+    J = SSD + 0.1 |m_K|^2.
+
+    - Against the FP32 oracle (the same forward arithmetic, so the same trajectory):
+      J within 1e-9, dJ/dlambda and dJ/dv0 within 1e-5 relative (the reverse sweeps add
+      in different orders).
+    - Against the FP64 oracle: J within 1e-5 and dJ/dlambda within 1e-4 relative; dJ/dv0
+      no further from it than the FP32 oracle is.  FP32 and FP64 trajectories put a few
+      sample positions on different sides of a cell face, where the interpolant's slope
+      jumps: about 1000 of the 6.3 M components carry nearly all of that distance
+      (6.4e-4 in L2 for either FP32 computation).
+    - Against central finite differences of the FP64 forward, every relative error <= 1e-4:
+      at lambda, along a random direction over 64 voxels, and at 8 voxel components with
+      large gradients.  J is piecewise smooth (a kink wherever a sample crosses a cell
+      face); a difference whose step straddles a kink measures a mix of two slopes, so each
+      check tries eps = 1e-3 first and then smaller steps, down to where the FP64 forward's
+      rounding would show."""
+    import json
+    import os
+    import torch
+    from fastreg_gb300 import synthetic as sy
+    dims = (128, 128, 128)
+    d = sy.make_pair(sy.PairSpec(dims=dims, n_blobs=40, vel_sigma=4.0, max_disp=4.0, n_classes=4, seed=4000))
+    P = Params(volume_dims=dims, solver="sobolev", smooth_sigma=1.5, smooth_width=7, damping=0.9, step=0.5)
+    v0 = (0.05 * rng(4001).normal(0.0, 1.0, (3,) + dims[::-1])).astype(np.float32)
+    lam, K, ck = 0.2, 50, 10
+    T, S = (torch.from_numpy(d[k]).to(cuda) for k in ("T", "S"))
+    J, gv_t, gl = _loss_grad(T, S, torch.from_numpy(v0).to(cuda), lam, K, ck, P)
+    gv = gv_t.cpu().numpy().astype(np.float64)
+    v64 = v0.astype(np.float64)
+    J64, gv64, gl64 = O.sob_loss_grad(P, d["T"], d["S"], v64, lam, K)
+    J32, gv32, gl32 = O.sob_loss_grad(P, d["T"], d["S"], v0, lam, K, True, prec=32)
+    gv32 = gv32.astype(np.float64)
+
+    def fwd(v, l):
+        return O.sob_loss_grad(P, d["T"], d["S"], v, l, K, False)[0]
+
+    def fd(f, target, steps):
+        """central differences of f at each step until one is within 1e-4 of target"""
+        tried = {}
+        for eps in steps:
+            g = (f(eps) - f(-eps)) / (2 * eps)
+            tried[eps] = abs(target - g) / abs(g)
+            if tried[eps] <= 1e-4:
+                break
+        return tried
+
+    l2 = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    rec = {"J_rel_fp32": abs(J - J32) / abs(J32), "dlambda_rel_fp32": abs(gl - gl32) / abs(gl32),
+           "dv0_rel_l2_fp32": l2(gv, gv32),
+           "J_rel_fp64": abs(J - J64) / abs(J64), "dlambda_rel_fp64": abs(gl - gl64) / abs(gl64),
+           "dv0_rel_l2_fp64": l2(gv, gv64), "dv0_rel_l2_fp32_oracle_vs_fp64": l2(gv32, gv64)}
+    rec["fd_lambda"] = fd(lambda e: fwd(v64, lam + e), gl, (1e-3, 1e-5, 1e-7, 1e-8, 1e-9, 1e-10))
+    r = rng(4002)
+    direction = np.zeros_like(v64)
+    flat = r.choice(v64[0].size, 64, replace=False)
+    for c in range(3):
+        direction[c].flat[flat] = r.choice([-1.0, 1.0], 64)
+    rec["fd_direction_64_voxels"] = fd(lambda e: fwd(v64 + e * direction, lam), float((gv * direction).sum()),
+                                       (1e-3, 1e-5, 1e-7, 1e-8))
+    big = np.flatnonzero(np.abs(gv64) >= 0.1 * np.abs(gv64).max())
+    rec["fd_voxels"] = {}
+    for idx in r.choice(big, 8, replace=False):
+        e_i = np.zeros(v64.size)
+        e_i[idx] = 1.0
+        e_i = e_i.reshape(v64.shape)
+        rec["fd_voxels"][int(idx)] = fd(lambda e: fwd(v64 + e * e_i, lam), float(gv.flat[idx]), (1e-3, 1e-5, 1e-7))
+    print(json.dumps(rec))
+    out = os.environ.get("FASTREG_RECORD_DIR")
+    if out:
+        with open(os.path.join(out, "adjoint_128cube.json"), "w") as f:
+            json.dump(rec, f, indent=1)
+    assert rec["J_rel_fp32"] <= 1e-9
+    assert rec["dlambda_rel_fp32"] <= 1e-5
+    assert rec["dv0_rel_l2_fp32"] <= 1e-5
+    assert rec["J_rel_fp64"] <= 1e-5
+    assert rec["dlambda_rel_fp64"] <= 1e-4
+    assert rec["dv0_rel_l2_fp64"] <= 1.02 * rec["dv0_rel_l2_fp32_oracle_vs_fp64"] + 1e-6
+    assert min(rec["fd_lambda"].values()) <= 1e-4, rec["fd_lambda"]
+    assert min(rec["fd_direction_64_voxels"].values()) <= 1e-4, rec["fd_direction_64_voxels"]
+    for k, v in rec["fd_voxels"].items():
+        assert min(v.values()) <= 1e-4, (k, v)

@@ -14,12 +14,13 @@ def _to(dev, a):
     return torch.from_numpy(np.ascontiguousarray(a)).to(dev)
 
 
+@pytest.mark.parametrize("staging", [1, 2])
 @pytest.mark.parametrize("solver", ["reference", "sobolev"])
-def test_batch_equals_pairs_alone(cuda, solver):
+def test_batch_equals_pairs_alone(cuda, solver, staging):
     """A cohort of uneven pairs in one set of launches gives, pair by pair, the bits
-    of each pair registered alone (and of the oracle)."""
+    of each pair registered alone (and of the oracle), with either staging."""
     dims_list = [(20, 18, 16), (33, 17, 21), (16, 24, 12), (40, 9, 10), (4, 4, 5)]
-    kw = dict(no_labels=4, max_iter=25, alpha=0.02, solver=solver, step=0.5, damping=0.9)
+    kw = dict(no_labels=4, max_iter=25, alpha=0.02, solver=solver, step=0.5, damping=0.9, staging=staging)
     pairs_np = [images(d, 50 + k) for k, d in enumerate(dims_list)]
     P = Params(volume_dims=dims_list[0], **kw)
     fr = FastReg(P)
@@ -45,11 +46,12 @@ def test_batch_equals_pairs_alone(cuda, solver):
         assert st.iterations == 25
 
 
+@pytest.mark.parametrize("staging", [1, 2])
 @pytest.mark.parametrize("dims", [(4, 5, 4), (12, 10, 9), (33, 17, 20)])
-def test_sobolev_registration(cuda, dims):
+def test_sobolev_registration(cuda, dims, staging):
     d = images(dims, 11 + dims[0])
     P = Params(volume_dims=dims, no_labels=4, max_iter=30, solver="sobolev", smooth_sigma=1.5, smooth_width=7,
-               damping=0.9, step=0.5)
+               damping=0.9, step=0.5, staging=staging)
     fr = FastReg(P)
     iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
     fr(iT, lT, iS, lS)
@@ -72,15 +74,17 @@ def test_sobolev_registration(cuda, dims):
     assert err < 1e-3, f"phi vs FP64 oracle: max abs err {err} voxels"
 
 
-@pytest.mark.parametrize("width", [1, 3, 9, 11, 15])
-def test_sobolev_smoothing_widths(cuda, width):
-    """Every smoothing radius (one kernel instance per radius: 16-byte staging with an x
-    halo of 4 or 8 columns, 3 or 2 staging buffers, clamped columns on edge tiles) gives
-    the oracle's bits; odd sizes put most tiles on an x edge."""
+@pytest.mark.parametrize("staging", [1, 2])
+@pytest.mark.parametrize("width", [1, 3, 5, 7, 9, 11, 13, 15])
+def test_sobolev_smoothing_widths(cuda, width, staging):
+    """Every smoothing radius with either staging (one kernel instance per radius and
+    staging: cp.async or TMA copies, an x halo of 4 or 8 columns, 2 to 4 staging buffers,
+    clamped rows and columns at the volume's edges) gives the oracle's bits; odd sizes put
+    most tiles on an x edge."""
     dims = (37, 19, 23)
     d = images(dims, 300 + width)
     P = Params(volume_dims=dims, no_labels=4, max_iter=6, solver="sobolev", smooth_sigma=0.4 + 0.3 * width,
-               smooth_width=width, damping=0.9, step=0.5)
+               smooth_width=width, damping=0.9, step=0.5, staging=staging)
     fr = FastReg(P)
     iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
     fr(iT, lT, iS, lS)

@@ -40,23 +40,21 @@ CASES = [((12, 6, 6), "slab", 0), ((40, 36, 30), "random", 3), ((33, 17, 20), "r
 def test_fold_count_with_folds_present(cuda, dims, kind, seed):
     d = images(dims, 50 + seed)
     psi = slab_reversal(dims) if kind == "slab" else random_folded(dims, seed, disp=4.0)
-    # psi_inv: another rough map, so that T o psi_inv is a real gather too
-    pinv = random_folded(dims, seed + 100, disp=1.0) if kind != "slab" else identity(dims)
     P = Params(volume_dims=dims, no_labels=4, max_iter=4, alpha=0.05)
     fr = FastReg(P)
     iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
     fr.begin([(iT, lT, iS, lS)])
     fr.set_field(N.FR_FIELD_PSI, _to(cuda, psi))
-    fr.set_field(N.FR_FIELD_PSI_INV, _to(cuda, pinv))
     fr.finish()
     st = fr.stats()
 
     out_S, out_labS = O.warp(psi, d["S"], d["labS"])
-    out_T, out_labT = O.warp(pinv, d["T"], d["labT"])
     assert_bitexact(iS.cpu().numpy(), out_S, "S o psi")
     assert_bitexact(lS.cpu().numpy(), out_labS, "labels S o psi")
-    assert_bitexact(iT.cpu().numpy(), out_T, "T o psi_inv")
-    assert_bitexact(lT.cpu().numpy(), out_labT, "labels T o psi_inv")
+    # no iteration ran: the target is left as it is (T o psi_inv is written by the
+    # iterations, src/fastreg/cuda/solver.cu:402)
+    assert_bitexact(iT.cpu().numpy(), d["T"], "T")
+    assert_bitexact(lT.cpu().numpy(), d["labT"], "labels T")
     os_ = O.stats(d["T"], d["labT"], out_S, out_labS, psi, P.no_labels)
     _, det = O.deformation_jacobian(psi)
     want = int((det <= 0).sum())

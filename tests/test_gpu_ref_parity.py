@@ -22,14 +22,19 @@ def _params(dims, **kw):
     return Params(**base)
 
 
+STAGINGS = [1, 2]  # STAGING: per-thread cp.async, TMA tensor copies
+
+
+@pytest.mark.parametrize("staging", STAGINGS)
 @pytest.mark.parametrize("dims", [(4, 4, 4), (5, 6, 4), (7, 9, 11), (33, 17, 20), (40, 36, 30)])
 @pytest.mark.parametrize("iter_no", [1, 2, 7])
-def test_one_iteration_from_random_state(cuda, dims, iter_no):
-    """One iteration (L, pass A, pass B) from a random mid-registration state."""
+def test_one_iteration_from_random_state(cuda, dims, iter_no, staging):
+    """One iteration (L, pass A, pass B) from a random mid-registration state, with
+    either staging of the stencil operands."""
     seed = 10 * dims[0] + iter_no
     d = images(dims, seed)
     st = random_state(dims, seed + 1, disp=1.5, vel=0.3)
-    P = _params(dims)
+    P = _params(dims, staging=staging)
     fr = FastReg(P)
     tens = [_to(cuda, d[k]) for k in ("T", "labT", "S", "labS")]
     fr.begin([tuple(tens)])
@@ -59,12 +64,14 @@ def test_one_iteration_from_random_state(cuda, dims, iter_no):
     fr.close()
 
 
+@pytest.mark.parametrize("staging", STAGINGS)
 @pytest.mark.parametrize("dims,iters", [((4, 5, 4), 20), ((12, 10, 9), 30), ((24, 20, 18), 60), ((64, 64, 64), 200)])
-def test_full_registration(cuda, dims, iters):
-    """A whole registration through FastReg::operator() semantics (in place)."""
+def test_full_registration(cuda, dims, iters, staging):
+    """A whole registration through FastReg::operator() semantics (in place), with either
+    staging of the stencil operands."""
     import torch
     d = images(dims, 7 + dims[0])
-    P = _params(dims, max_iter=iters, alpha=0.02)
+    P = _params(dims, max_iter=iters, alpha=0.02, staging=staging)
     fr = FastReg(P)
     iT, lT, iS, lS = (_to(cuda, d[k]) for k in ("T", "labT", "S", "labS"))
     assert fr(iT, lT, iS, lS)
@@ -75,6 +82,7 @@ def test_full_registration(cuda, dims, iters):
 
     o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
     assert st.iterations == o["iterations"] == iters
+    assert fr.tile_staging()[0] == ("tma" if staging == 2 else "cp.async")
     assert_bitexact(psi_g, o["psi"], "psi")
     assert_bitexact(pinv_g, o["psi_inv"], "psi_inv")
     assert_bitexact(iT.cpu().numpy(), o["out_T"], "T o psi_inv")

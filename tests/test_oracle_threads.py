@@ -1,6 +1,7 @@
 """The oracle's OpenMP loops do not change any result: a reference-mode and a sobolev
 registration, run in child processes with 1 and with 3 threads, give the same bits
-(fields, warped images and labels, max-update traces with their voxels, FP64 energies)."""
+(fields, warped images and labels, max-update traces with their voxels, FP64 energies),
+and so does the FP64 adjoint of an unrolled sobolev registration."""
 import os
 import subprocess
 import sys
@@ -23,7 +24,10 @@ o = O.ref_register(P, d["T"], d["labT"], d["S"], d["labS"])
 Ps = Params(volume_dims=dims, no_labels=4, max_iter=15, solver="sobolev", smooth_sigma=1.5, smooth_width=7,
             damping=0.9, step=0.5)
 s = O.sob_register(Ps, d["T"], d["S"])
-np.savez(sys.argv[2], psi=o["psi"], psi_inv=o["psi_inv"], out_S=o["out_S"], out_labS=o["out_labS"],
+from tests.helpers import rng, smooth_noise
+v0 = smooth_noise(rng(5), (3,) + dims[::-1], 0.3).astype(np.float64)
+J, gv, gl = O.sob_loss_grad(Ps, d["T"], d["S"], v0, 0.2, 6)
+np.savez(sys.argv[2], adj_J=np.float64(J), adj_gv=gv, adj_gl=np.float64(gl), psi=o["psi"], psi_inv=o["psi_inv"], out_S=o["out_S"], out_labS=o["out_labS"],
          out_T=o["out_T"], tn=o["trace_norm"], ti=o["trace_idx"], phi=s["phi"], m=s["m"], stn=s["trace_norm"],
          sti=s["trace_idx"], ste=s["trace_energy"])
 """
