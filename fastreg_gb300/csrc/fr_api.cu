@@ -239,7 +239,7 @@ std::vector<int> active_roles(const fr_handle* h) {
 }
 
 // kernels with a TMA-staged variant
-bool has_tma_variant(int r) { return r == R_LAP || r == R_SG || r == R_SS; }
+bool has_tma_variant(int r) { return r == R_LAP || r == R_PA || r == R_SG || r == R_SS; }
 
 // the staging variants kernel r may run with this handle's STAGING and cohort
 std::vector<int> allowed_variants(const fr_handle* h, int r) {
@@ -251,7 +251,7 @@ std::vector<int> allowed_variants(const fr_handle* h, int r) {
 const void* role_fn(const fr_handle* h, int r, int variant = 0) {
     switch (r) {
         case R_LAP: return variant ? (const void*)frg::ref_laplacian_tma_kernel : (const void*)frg::ref_laplacian_kernel;
-        case R_PA: return (const void*)frg::ref_pass_a_kernel;
+        case R_PA: return variant ? (const void*)frg::ref_pass_a_tma_kernel : (const void*)frg::ref_pass_a_kernel;
         case R_PB: return (const void*)frg::ref_pass_b_kernel;
         case R_SG: return variant ? (const void*)frg::sob_grad_tma_kernel : (const void*)frg::sob_grad_kernel;
         case R_SS: return frg::sob_smooth3_fn(h->P.smooth_width / 2, variant);
@@ -262,7 +262,7 @@ const void* role_fn(const fr_handle* h, int r, int variant = 0) {
 size_t role_smem(int r, int variant = 0) {
     switch (r) {
         case R_LAP: return variant ? frg::ref_laplacian_tma_smem_bytes() : frg::ref_laplacian_smem_bytes();
-        case R_PA: return frg::ref_pass_a_smem_bytes();
+        case R_PA: return variant ? frg::ref_pass_a_tma_smem_bytes() : frg::ref_pass_a_smem_bytes();
         case R_SG: return variant ? frg::sob_grad_tma_smem_bytes() : frg::sob_grad_smem_bytes();
         default: return 0;
     }
@@ -370,6 +370,19 @@ int encode_tmaps(fr_handle* h) {
             const cuuint64_t dims[3] = {Xp, Y, Z}, strides[2] = {4 * Xp, 4 * Xp * Y};
             const cuuint32_t box[3] = {32, 8, 1};
             int rc = encode_map(h, m + frg::TM_LAP_T, h->T + P.off, 3, dims, strides, box);
+            if (rc != FR_OK) return rc;
+        }
+        if (h->P.solver == FR_SOLVER_REFERENCE) {  // pass A's v, psi_inv, rho (both buffers) and S
+            const cuuint64_t d4[4] = {Xp, Y, Z, 3}, s4[3] = {4 * Xp, 4 * Xp * Y, fstride};
+            const cuuint64_t d3[3] = {Xp, Y, Z}, s3[2] = {4 * Xp, 4 * Xp * Y};
+            const cuuint32_t bv[4] = {40, 12, 1, 3}, bq[4] = {40, 10, 1, 3}, b3[3] = {40, 10, 1};
+            for (int k = 0; k < 2; ++k) {
+                int rc = encode_map(h, m + frg::TM_PA_V0 + k, h->v[k] + P.off, 4, d4, s4, bv);
+                if (rc == FR_OK) rc = encode_map(h, m + frg::TM_PA_Q0 + k, h->pinv[k] + P.off, 4, d4, s4, bq);
+                if (rc == FR_OK) rc = encode_map(h, m + frg::TM_PA_R0 + k, h->rho[k] + P.off, 3, d3, s3, b3);
+                if (rc != FR_OK) return rc;
+            }
+            int rc = encode_map(h, m + frg::TM_PA_S, h->S + P.off, 3, d3, s3, b3);
             if (rc != FR_OK) return rc;
         }
         if (h->P.solver == FR_SOLVER_SOBOLEV) {
@@ -500,10 +513,14 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     FR_CUDA(h, cudaMemset(h->block, 0, total));
     FR_CUDA(h, cudaMemcpy(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice));
     FR_CUDA(h, cudaMemcpy(h->d_tiles, h->htiles.data(), sizeof(Tile) * ntiles, cudaMemcpyHostToDevice));
-    if (h->P.solver == FR_SOLVER_REFERENCE)
+    if (h->P.solver == FR_SOLVER_REFERENCE) {
         FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)frg::ref_pass_a_smem_bytes()));
+        FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_tma_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)frg::ref_pass_a_tma_smem_bytes()));
+    }
     h->tma_ok = encode_tmaps(h) == FR_OK;
     if (!h->tma_ok && h->P.staging == 2) {
         const std::string why = h->err;
@@ -583,7 +600,10 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
     else
         frg::ref_laplacian_kernel<<<h->ts[R_LAP].grid, 256, frg::ref_laplacian_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[1], s);
-    frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
+    if (h->ts[R_PA].shape.variant)
+        frg::ref_pass_a_tma_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_tma_smem_bytes(), s>>>(a);
+    else
+        frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
     frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);

@@ -18,6 +18,13 @@ enum TmapIndex {
                      // phi living where psi does)
     TM_SOB_G,        // the sobolev gradient g, 4-D, box (32 + 2 HX) x (8 + 2 R) x 1 x 3 for the
                      // smoothing radius R (HX = R rounded up to 4)
+    TM_PA_V0,        // pass A: v (buffer 0, 1), 4-D, box 40 x 12 x 1 x 3 (2-voxel halo)
+    TM_PA_V1,
+    TM_PA_Q0,        // psi_inv (buffer 0, 1), 4-D, box 40 x 10 x 1 x 3
+    TM_PA_Q1,
+    TM_PA_R0,        // rho (buffer 0, 1), 3-D, box 40 x 10 x 1
+    TM_PA_R1,
+    TM_PA_S,         // S, 3-D, box 40 x 10 x 1
     TM_COUNT
 };
 
@@ -63,6 +70,8 @@ size_t ref_laplacian_tma_smem_bytes();  // dynamic shared memory of ref_laplacia
 __global__ void ref_laplacian_tma_kernel(RefIterArgs a);
 size_t ref_pass_a_smem_bytes();  // dynamic shared memory of ref_pass_a_kernel
 __global__ void ref_pass_a_kernel(RefIterArgs a);
+size_t ref_pass_a_tma_smem_bytes();  // dynamic shared memory of ref_pass_a_tma_kernel
+__global__ void ref_pass_a_tma_kernel(RefIterArgs a);
 __global__ void ref_pass_b_kernel(RefIterArgs a);
 
 // Caller-owned buffers of one pair (device pointers); outputs overwrite inputs in place

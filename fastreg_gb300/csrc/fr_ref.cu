@@ -510,6 +510,147 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
 }
 
 // ----------------------------------------------------------------------------------
+// Pass A with TMA staging.  Per slice, one thread issues four tensor copies: v's box of 40
+// columns x 12 rows x 3 components (2-voxel halo) into the v ring, and psi_inv's 40 x 10 x
+// 3 box, rho's and S's 40 x 10 boxes into one slot of the psi_inv ring; each ring slot
+// completes on its own mbarrier.  The v ring holds the 5 slices z - 2 .. z + 2 and the
+// psi_inv ring the 3 slices z - 1 .. z + 1 that slice z reads, each with one more slice in
+// flight; one block barrier per slice frees the slots of slices z - 3 / z - 2 for the next
+// copies.  Out-of-volume parts of a box read as zero and are never used (the stencils
+// that reach them are masked, as in the cp.async kernel).  Waits are bounded as in
+// ref_laplacian_tma_kernel.  The voxel arithmetic is pass_a_voxel, shared with
+// ref_pass_a_kernel.
+// ----------------------------------------------------------------------------------
+namespace {
+constexpr int kPVS = 6, kPQS = 4;                 // ring slots: v (5 + 1), psi_inv/rho/S (3 + 1)
+constexpr int kPW = 40;                           // staged row: columns x0 - 4 .. x0 + 35
+constexpr int kPVPlane = kPW * 12, kPVSlot = 3 * kPVPlane;  // 1440 floats = 5760 bytes
+constexpr int kPQPlane = kPW * 10;
+constexpr int kPQR = 1216, kPQSo = 1632, kPQSlot = 2048;    // rho, S offsets; slot (floats)
+constexpr unsigned kPVBytes = sizeof(float) * kPVSlot;
+constexpr unsigned kPQBytes = sizeof(float) * (3 * kPQPlane + 2 * kPQPlane);
+static_assert((kPVSlot * 4) % 128 == 0 && (kPQR * 4) % 128 == 0 && (kPQSo * 4) % 128 == 0 &&
+                  3 * kPQPlane <= kPQR && kPQR + kPQPlane <= kPQSo && kPQSo + kPQPlane <= kPQSlot,
+              "slot layout");
+}  // namespace
+
+size_t ref_pass_a_tma_smem_bytes() {
+    return 128 + sizeof(float) * (kPVS * kPVSlot + kPQS * kPQSlot) + sizeof(uint64_t) * (kPVS + kPQS);
+}
+
+__global__ void __launch_bounds__(256, 3) ref_pass_a_tma_kernel(RefIterArgs a) {
+    extern __shared__ __align__(128) unsigned char pa_raw[];
+    float* vring = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(pa_raw) + 127) & ~uintptr_t(127));
+    float* qring = vring + kPVS * kPVSlot;
+    uint64_t* fullv = reinterpret_cast<uint64_t*>(qring + kPQS * kPQSlot);
+    uint64_t* fullq = fullv + kPVS;
+    typedef SliceRing<kPVS> VRing;
+    typedef SliceRing<kPQS> QRing;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+    if (tid == 0) {
+        for (int k = 0; k < kPVS; ++k) mbar_init(fullv + k, 1);
+        for (int k = 0; k < kPQS; ++k) mbar_init(fullq + k, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int src = (a.iter - 1) & 1;  // the buffers this iteration reads
+    unsigned nbv = 0, nbq = 0, iv = 0, iq = 0;  // fills before this tile; fills issued (thread 0)
+    bool failed = false;
+    for (int t = blockIdx.x; t < a.ntiles_a && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_a[t];
+        if (a.stop[tl.x]) continue;  // uniform over the block
+        const Pair P = a.pairs[tl.x];
+        const int X = P.X, Y = P.Y, Z = P.Z, N = (int)P.N;
+        const int Xp = P.Xp, XYp = P.Xp * P.Y;
+        const int zs0 = max(tl.w, 1), zs1 = min(tl.w + a.depth_a, Z - 1);
+        if (zs0 >= zs1 || tl.y + kTileX <= 1 || tl.z + kTileY <= 1 || tl.y >= X - 1 || tl.z >= Y - 1) continue;
+        const long long NT = a.NT;
+        const float* __restrict__ Vg[3] = {a.v + P.off, a.v + NT + P.off, a.v + 2 * NT + P.off};
+        const float* __restrict__ Rg = a.rho + P.off;
+        const float* __restrict__ Sg = a.S + P.off;
+        const float* __restrict__ Tg = a.T + P.off;
+        const float4* __restrict__ LT = a.LT + P.off;
+        float* rho_n = a.rho_n + P.off;
+        float* Vn[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
+        float* Qn[3] = {a.pinv_n + P.off, a.pinv_n + NT + P.off, a.pinv_n + 2 * NT + P.off};
+        const int pair = tl.x;
+        const int x0 = tl.y, y0 = tl.z;
+        const int x = x0 + tx, y = y0 + ty;
+        const bool active = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
+        const bool dv_xy = x >= 2 && x <= X - 3 && y >= 2 && y <= Y - 2;
+        const int nsteps = zs1 - zs0;
+        const int nv = nsteps + 4, nq = nsteps + 2;  // v slices zs0 - 2 .. zs1 + 1; psi_inv zs0 - 1 .. zs1
+        // the copies (thread 0 only); the maps' addresses are formed where they are used
+        auto issue_v = [&](int f) {
+            const unsigned n = nbv + (unsigned)f;
+            uint64_t* bar = fullv + VRing::slot(n);
+            const CUtensorMap* mv = a.tmaps + (long long)pair * TM_COUNT + TM_PA_V0 + src;
+            mbar_arrive_expect_tx(bar, kPVBytes);
+            tma_load_4d(vring + VRing::slot(n) * kPVSlot, mv, x0 - 4, y0 - 2, zs0 - 2 + f, 0, bar);
+            ++iv;
+        };
+        auto issue_q = [&](int f) {
+            const unsigned n = nbq + (unsigned)f;
+            uint64_t* bar = fullq + QRing::slot(n);
+            float* dst = qring + QRing::slot(n) * kPQSlot;
+            const CUtensorMap* maps = a.tmaps + (long long)pair * TM_COUNT;
+            const int z = zs0 - 1 + f;
+            mbar_arrive_expect_tx(bar, kPQBytes);
+            tma_load_4d(dst, maps + TM_PA_Q0 + src, x0 - 4, y0 - 1, z, 0, bar);
+            tma_load_3d(dst + kPQR, maps + TM_PA_R0 + src, x0 - 4, y0 - 1, z, bar);
+            tma_load_3d(dst + kPQSo, maps + TM_PA_S, x0 - 4, y0 - 1, z, bar);
+            ++iq;
+        };
+        __syncthreads();  // the previous tile is done with the rings
+        if (tid == 0) {
+            for (int f = 0; f < min(nv, kPVS); ++f) issue_v(f);
+            for (int f = 0; f < min(nq, kPQS); ++f) issue_q(f);
+        }
+        const int vc0 = (ty + 2) * kPW + tx + 4;
+        const int qc0 = (ty + 1) * kPW + tx + 4;
+        for (int j0 = 0; j0 < nsteps; ++j0) {
+            // slice z = zs0 + j0 reads v fills j0 .. j0 + 4 and psi_inv fills j0 .. j0 + 2
+            bool ok = true;
+            for (int f = (j0 == 0 ? 0 : j0 + 4); f <= j0 + 4; ++f)
+                ok = ok && mbar_wait_bounded(fullv + VRing::slot(nbv + f), VRing::parity(nbv + f));
+            for (int f = (j0 == 0 ? 0 : j0 + 2); f <= j0 + 2; ++f)
+                ok = ok && mbar_wait_bounded(fullq + QRing::slot(nbq + f), QRing::parity(nbq + f));
+            // every thread is past slice z - 1: the slots of v fill j0 - 1 and psi_inv fill
+            // j0 - 1 are free; the block agrees on whether any wait gave up
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0 && j0 >= 1) {
+                if (j0 - 1 + kPVS < nv) issue_v(j0 - 1 + kPVS);
+                if (j0 - 1 + kPQS < nq) issue_q(j0 - 1 + kPQS);
+            }
+            if (active) {
+                const int z = zs0 + j0;
+                const int i = x + Xp * y + XYp * z;
+                const float* vb[5];
+#pragma unroll
+                for (int k = 0; k < 5; ++k) vb[k] = vring + VRing::slot(nbv + j0 + k) * kPVSlot + vc0;
+                const float* qb[3];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) qb[k] = qring + QRing::slot(nbq + j0 + k) * kPQSlot + qc0;
+                pass_a_voxel<kPVPlane, kPQPlane, kPQR, kPQSo, kPW>(a, P, X, Y, Z, N, Xp, XYp, y, z, i, dv_xy, vb, qb,
+                                                                   LT, Tg, Sg, Rg, Vg, rho_n, Vn, Qn);
+            }
+        }
+        nbv += (unsigned)nv;  // every fill of the tile has been waited for
+        nbq += (unsigned)nq;
+    }
+    if (failed && tid == 0) {
+        for (unsigned n = (iv > (unsigned)kPVS ? iv - kPVS : 0u); n < iv; ++n)
+            mbar_wait_bounded(fullv + VRing::slot(n), VRing::parity(n));
+        for (unsigned n = (iq > (unsigned)kPQS ? iq - kPQS : 0u); n < iq; ++n)
+            mbar_wait_bounded(fullq + QRing::slot(n), QRing::parity(n));
+        atomicOr(a.err, kErrTmaTimeout);
+    }
+}
+
+// ----------------------------------------------------------------------------------
 // pass B: psi += alpha * v o psi, max update norm, convergence
 // ----------------------------------------------------------------------------------
 __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
