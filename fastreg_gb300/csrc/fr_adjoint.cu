@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 #include "../../include/fastreg_gb300.h"
@@ -113,6 +114,39 @@ __device__ __forceinline__ void lap_u(const AdjDims& D, const float* __restrict_
 
 #define GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
+// Grid-stride loop over whole warps: every lane of a warp runs the same iterations (lane
+// i of a warp holds voxel base + i; `act` is false past the end), so the body may use
+// warp shuffles.
+#define WARP_STRIDE(i, act, n)                                                                  \
+    for (int i##_w = blockIdx.x * blockDim.x + (threadIdx.x & ~31); i##_w < (n);                  \
+         i##_w += gridDim.x * blockDim.x)                                                        \
+        for (int i = i##_w + (threadIdx.x & 31), act = i < (n), i##_once = 1; i##_once; i##_once = 0)
+
+// Scatter-add of one cell's eight corner contributions cw[q] (q: bit 0 x, bit 1 y, bit 2 z;
+// the corners of tri_eval) into F, with the corners that neighbouring lanes share added
+// once: the lanes of a warp hold consecutive voxels of a row, whose cells are usually
+// consecutive along x (a smooth map), so lane k's x + 1 corners are lane k + 1's x corners.
+// Lane k then adds lane k - 1's x + 1 contribution to its own x one (one atomic for both),
+// halving the atomics of such runs.  All 32 lanes must call it; inactive lanes pass
+// act = false.
+__device__ __forceinline__ void scatter_cell_warp(float* F, int b, const float cw[8], bool act, int X, int XY) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int bprev = __shfl_up_sync(full, act ? b : -4, 1);
+    const bool merge = act && lane > 0 && bprev == b - 1;
+    const bool next_merges = __shfl_down_sync(full, (int)merge, 1) != 0 && lane < 31;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int o = ((j & 1) ? X : 0) + ((j & 2) ? XY : 0);
+        const float c0 = cw[2 * j], c1 = cw[2 * j + 1];
+        const float c1prev = __shfl_up_sync(full, c1, 1);
+        if (act) {
+            atomicAdd(F + b + o, merge ? c0 + c1prev : c0);
+            if (!next_merges) atomicAdd(F + b + 1 + o, c1);
+        }
+    }
+}
+
 // ---- forward (same arithmetic as the cohort kernels and the oracle) ----
 __global__ void adj_fwd_grad_kernel(AdjDims D, const float* __restrict__ S, const float* __restrict__ T,
                                     const float* __restrict__ phi, float lambda, float* __restrict__ g) {
@@ -193,24 +227,29 @@ __global__ void adj_loss_kernel(AdjDims D, const float* __restrict__ S, const fl
     if (threadIdx.x == 0) atomicAdd(loss, e);
 }
 
-// phi' = phi + m'(phi): pbar_k = pbar + (dm'/dphi)^T pbar, mbar += scatter(w * pbar)
+// phi' = phi + m'(phi): pbar_k = pbar + (dm'/dphi)^T pbar, mbar += scatter(w * pbar), the
+// scatter warp-aggregated (scatter_cell_warp)
 __global__ void adj_update_kernel(AdjDims D, const float* __restrict__ phi, const float* __restrict__ mn,
                                   const float* __restrict__ pbar, float* pbar_k, float* mbar) {
-    GRID_STRIDE(i, D.N) {
-        const float p[3] = {__ldg(phi + i), __ldg(phi + D.N + i), __ldg(phi + 2 * D.N + i)};
-        float acc[3] = {__ldg(pbar + i), __ldg(pbar + D.N + i), __ldg(pbar + 2 * D.N + i)};
+    WARP_STRIDE(i, act, D.N) {
+        const int k = act ? i : 0;
+        const float p[3] = {__ldg(phi + k), __ldg(phi + D.N + k), __ldg(phi + 2 * D.N + k)};
+        float acc[3] = {__ldg(pbar + k), __ldg(pbar + D.N + k), __ldg(pbar + 2 * D.N + k)};
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             TriEval t;
             tri_eval(D, mn + (long long)c * D.N, p[0], p[1], p[2], t, false);
-            const float pb = __ldg(pbar + (long long)c * D.N + i);
+            const float pb = __ldg(pbar + (long long)c * D.N + k);
 #pragma unroll
             for (int j = 0; j < 3; ++j) acc[j] += pb * t.d[j];
+            float cw[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) atomicAdd(mbar + (long long)c * D.N + t.off[q], t.w[q] * pb);
+            for (int q = 0; q < 8; ++q) cw[q] = t.w[q] * pb;
+            scatter_cell_warp(mbar + (long long)c * D.N, t.off[0], cw, act, D.X, D.XY);
         }
+        if (act)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) pbar_k[(long long)j * D.N + i] = acc[j];
+            for (int j = 0; j < 3; ++j) pbar_k[(long long)j * D.N + i] = acc[j];
     }
 }
 
@@ -342,6 +381,64 @@ struct AdjBuffers {
     size_t floats = 0;
 };
 
+// The device workspace of fr_sobolev_loss_grad (checkpoints, segment states and adjoint
+// fields, about 40 fields of 3 N floats for 50 iterations), kept per device and reused by
+// later calls that need as much or less: an unrolled registration is typically
+// differentiated many times in a row (hypergradient steps), and a fresh cudaMalloc /
+// cudaFree of a gigabyte per call costs milliseconds and synchronises the device.  A call
+// that finds the workspace busy (another host thread's call on the same device) uses a
+// private allocation instead.
+std::mutex g_ws_mu;
+struct Workspace {
+    float* ptr = nullptr;
+    size_t floats = 0;
+    bool busy = false;
+};
+Workspace g_ws[64];
+
+// a workspace of at least `floats` floats on device `dev`; *cached says whether it is the
+// shared one (released with release_workspace) or private (freed by the caller)
+float* acquire_workspace(int dev, size_t floats, bool* cached) {
+    *cached = false;
+    if (dev >= 0 && dev < 64) {
+        std::lock_guard<std::mutex> lk(g_ws_mu);
+        Workspace& w = g_ws[dev];
+        if (!w.busy) {
+            if (w.floats < floats) {
+                if (w.ptr) cudaFree(w.ptr);
+                w.ptr = nullptr;
+                w.floats = 0;
+                if (cudaMalloc((void**)&w.ptr, floats * sizeof(float)) == cudaSuccess)
+                    w.floats = floats;
+                else {
+                    cudaGetLastError();
+                    w.ptr = nullptr;
+                }
+            }
+            if (w.ptr) {
+                w.busy = true;
+                *cached = true;
+                return w.ptr;
+            }
+        }
+    }
+    float* p = nullptr;
+    if (cudaMalloc((void**)&p, floats * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void release_workspace(int dev, float* p, bool cached) {
+    if (!cached) {
+        cudaFree(p);
+        return;
+    }
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    g_ws[dev].busy = false;
+}
+
 int grid_for(long long n) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -389,9 +486,15 @@ extern "C" int fr_sobolev_loss_grad(const float* d_T, const float* d_S, const in
     // buffers: checkpoints (phi, m) x nck, segment states (phi_k, m_{k+1}) x ck, working phi, m,
     // g, tmp, adjoint pbar, pbar_k, mbar, gbar (+ 2 doubles)
     const size_t floats = N3 * (2 * nck + 2 * ck + 8) + 64;
-    float* blk = nullptr;
-    if (cudaMalloc((void**)&blk, floats * sizeof(float)) != cudaSuccess) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
+        set_global_error("fr_sobolev_loss_grad: no current CUDA device");
+        return FR_ERR_CUDA;
+    }
+    bool cached = false;
+    float* blk = acquire_workspace(dev, floats, &cached);
+    if (!blk) {
         set_global_error("fr_sobolev_loss_grad: device allocation failed");
         return FR_ERR_ALLOC;
     }
@@ -463,7 +566,8 @@ extern "C" int fr_sobolev_loss_grad(const float* d_T, const float* d_S, const in
             cudaStreamSynchronize(s) != cudaSuccess)
             rc = FR_ERR_CUDA;
     }
-    cudaFree(blk);
+    if (rc != FR_OK) cudaStreamSynchronize(s);  // nothing may still use the workspace
+    release_workspace(dev, blk, cached);
     if (rc != FR_OK) {
         cudaGetLastError();
         set_global_error("fr_sobolev_loss_grad: a CUDA call failed");
@@ -480,16 +584,20 @@ extern "C" int fr_warp_adjoint(const float* d_pos, const float* d_img, const flo
 namespace frg {
 __global__ void warp_adjoint_kernel(AdjDims D, const float* __restrict__ pos, const float* __restrict__ img,
                                     const float* __restrict__ wbar, float* pos_bar, float* img_bar) {
-    GRID_STRIDE(i, D.N) {
+    WARP_STRIDE(i, act, D.N) {
+        const int k = act ? i : 0;
         TriEval t;
-        tri_eval(D, img, __ldg(pos + i), __ldg(pos + D.N + i), __ldg(pos + 2 * D.N + i), t, false);
-        const float wb = __ldg(wbar + i);
-        if (pos_bar)
+        tri_eval(D, img, __ldg(pos + k), __ldg(pos + D.N + k), __ldg(pos + 2 * D.N + k), t, false);
+        const float wb = __ldg(wbar + k);
+        if (pos_bar && act)
 #pragma unroll
             for (int j = 0; j < 3; ++j) pos_bar[(long long)j * D.N + i] = wb * t.d[j];
-        if (img_bar)
+        if (img_bar) {  // uniform: every lane calls the warp scatter
+            float cw[8];
 #pragma unroll
-            for (int q = 0; q < 8; ++q) atomicAdd(img_bar + t.off[q], t.w[q] * wb);
+            for (int q = 0; q < 8; ++q) cw[q] = t.w[q] * wb;
+            scatter_cell_warp(img_bar, t.off[0], cw, act, D.X, D.XY);
+        }
     }
 }
 }  // namespace frg

@@ -239,7 +239,7 @@ std::vector<int> active_roles(const fr_handle* h) {
 }
 
 // kernels with a TMA-staged variant
-bool has_tma_variant(int r) { return r == R_LAP || r == R_PA || r == R_SG || r == R_SS; }
+bool has_tma_variant(int r) { return r != R_COUNT; }  // every solver kernel has one
 
 // the staging variants kernel r may run with this handle's STAGING and cohort
 std::vector<int> allowed_variants(const fr_handle* h, int r) {
@@ -252,10 +252,10 @@ const void* role_fn(const fr_handle* h, int r, int variant = 0) {
     switch (r) {
         case R_LAP: return variant ? (const void*)frg::ref_laplacian_tma_kernel : (const void*)frg::ref_laplacian_kernel;
         case R_PA: return variant ? (const void*)frg::ref_pass_a_tma_kernel : (const void*)frg::ref_pass_a_kernel;
-        case R_PB: return (const void*)frg::ref_pass_b_kernel;
+        case R_PB: return variant ? (const void*)frg::ref_pass_b_staged_kernel : (const void*)frg::ref_pass_b_kernel;
         case R_SG: return variant ? (const void*)frg::sob_grad_tma_kernel : (const void*)frg::sob_grad_kernel;
         case R_SS: return frg::sob_smooth3_fn(h->P.smooth_width / 2, variant);
-        default: return (const void*)frg::sob_pass_b_kernel;
+        default: return variant ? (const void*)frg::sob_pass_b_staged_kernel : (const void*)frg::sob_pass_b_kernel;
     }
 }
 
@@ -264,6 +264,8 @@ size_t role_smem(int r, int variant = 0) {
         case R_LAP: return variant ? frg::ref_laplacian_tma_smem_bytes() : frg::ref_laplacian_smem_bytes();
         case R_PA: return variant ? frg::ref_pass_a_tma_smem_bytes() : frg::ref_pass_a_smem_bytes();
         case R_SG: return variant ? frg::sob_grad_tma_smem_bytes() : frg::sob_grad_smem_bytes();
+        case R_PB:
+        case R_SB: return variant ? frg::gather_staged_smem_bytes() : 0;
         default: return 0;
     }
 }
@@ -384,6 +386,16 @@ int encode_tmaps(fr_handle* h) {
             }
             int rc = encode_map(h, m + frg::TM_PA_S, h->S + P.off, 3, d3, s3, b3);
             if (rc != FR_OK) return rc;
+        }
+        {  // the gathered field of the update kernel: v (both buffers) or the momentum
+            const cuuint64_t d4[4] = {Xp, Y, Z, 3}, s4[3] = {4 * Xp, 4 * Xp * Y, fstride};
+            const cuuint32_t bg[4] = {frg::kGBX, frg::kGBY, frg::kGBZ, 3};
+            const int nb = h->P.solver == FR_SOLVER_REFERENCE ? 2 : 1;
+            for (int k = 0; k < nb; ++k) {
+                int rc = encode_map(h, m + (nb == 2 ? frg::TM_PB_V0 + k : frg::TM_SB_M), h->v[k] + P.off, 4, d4, s4,
+                                    bg);
+                if (rc != FR_OK) return rc;
+            }
         }
         if (h->P.solver == FR_SOLVER_SOBOLEV) {
             int wx = 0, rows = 0;
@@ -521,6 +533,9 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)frg::ref_pass_a_tma_smem_bytes()));
     }
+    FR_CUDA(h, cudaFuncSetAttribute(role_fn(h, h->P.solver == FR_SOLVER_REFERENCE ? R_PB : R_SB, 1),
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)frg::gather_staged_smem_bytes()));
     h->tma_ok = encode_tmaps(h) == FR_OK;
     if (!h->tma_ok && h->P.staging == 2) {
         const std::string why = h->err;
@@ -605,7 +620,10 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
     else
         frg::ref_pass_a_kernel<<<h->ts[R_PA].grid, 256, frg::ref_pass_a_smem_bytes(), s>>>(a);
     if (ev) cudaEventRecord(ev[2], s);
-    frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, 256, 0, s>>>(a);
+    if (h->ts[R_PB].shape.variant)
+        frg::ref_pass_b_staged_kernel<<<h->ts[R_PB].grid, 256, frg::gather_staged_smem_bytes(), s>>>(a);
+    else
+        frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);
     FR_LAUNCHED(h);
     return FR_OK;
@@ -654,7 +672,7 @@ int launch_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t* ev
     if (h->P.solver == FR_SOLVER_REFERENCE) return launch_ref_iter(h, iter, t, s, ev);
     const frg::SobIterArgs a = sob_args(h, iter);
     const int grids[3] = {h->ts[R_SG].grid, h->ts[R_SS].grid, h->ts[R_SB].grid};
-    const int variants[2] = {h->ts[R_SG].shape.variant, h->ts[R_SS].shape.variant};
+    const int variants[3] = {h->ts[R_SG].shape.variant, h->ts[R_SS].shape.variant, h->ts[R_SB].shape.variant};
     cudaError_t e = frg::launch_sob_iter(a, grids, variants, s, ev);
     if (e != cudaSuccess) return fail(h, FR_ERR_CUDA, "sobolev launch failed: %s", cudaGetErrorString(e));
     return FR_OK;

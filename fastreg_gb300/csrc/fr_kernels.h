@@ -25,8 +25,16 @@ enum TmapIndex {
     TM_PA_R0,        // rho (buffer 0, 1), 3-D, box 40 x 10 x 1
     TM_PA_R1,
     TM_PA_S,         // S, 3-D, box 40 x 10 x 1
+    TM_PB_V0,        // pass B's gathered v (buffer 0, 1), 4-D, box kGBX x kGBY x kGBZ x 3
+    TM_PB_V1,
+    TM_SB_M,         // the sobolev update's gathered momentum, 4-D, the same box
     TM_COUNT
 };
+
+// The box of a staged gather (pass B of either solver): columns, rows and slices of the
+// gathered field copied per slice of a tile, enough for the cells of a 32 x 8 slice of a
+// smooth map (the box's x origin is the cells' lowest x rounded down to a multiple of 4).
+constexpr int kGBX = 48, kGBY = 12, kGBZ = 4;
 
 // Arguments of one reference-mode iteration (all three launches take the same block).
 struct RefIterArgs {
@@ -73,6 +81,8 @@ __global__ void ref_pass_a_kernel(RefIterArgs a);
 size_t ref_pass_a_tma_smem_bytes();  // dynamic shared memory of ref_pass_a_tma_kernel
 __global__ void ref_pass_a_tma_kernel(RefIterArgs a);
 __global__ void ref_pass_b_kernel(RefIterArgs a);
+size_t gather_staged_smem_bytes();  // dynamic shared memory of the staged-gather pass B kernels
+__global__ void ref_pass_b_staged_kernel(RefIterArgs a);
 
 // Caller-owned buffers of one pair (device pointers); outputs overwrite inputs in place
 // exactly like FastReg::operator() (src/fastreg/fastreg.cpp:58-75).

@@ -732,4 +732,180 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
     if (tid == 0) *a.counter = 0u;
 }
 
+
+// ----------------------------------------------------------------------------------
+// Pass B with the gathered neighbourhood staged in shared memory.  Per slice of its tile
+// the block reduces the bounding box of its voxels' cells (cellbox_add) and, when the
+// cells fit a kGBX x kGBY x kGBZ box, one thread copies that box of v's three components
+// with one tensor copy; the corners are then read from shared memory.  The copy of slice
+// z + 1's box is issued while slice z is gathered (two buffers), and the slice's one block
+// barrier both publishes the next box and frees the buffer of slice z - 1.  Voxels whose
+// cell has a corner outside the grid (they read element 0, as get_global_idx does) and
+// slices whose cells do not fit the box gather from global memory as ref_pass_b_kernel
+// does; the arithmetic is the same.  Waits are bounded (about a second); a block that gives
+// up sets the device error word.
+// ----------------------------------------------------------------------------------
+namespace {
+constexpr int kGBPlane = kGBX * kGBY * kGBZ;  // one component of a box (floats)
+constexpr unsigned kGBBytes = sizeof(float) * 3 * kGBPlane;
+}  // namespace
+
+size_t gather_staged_smem_bytes() { return 128 + 2 * (size_t)kGBBytes + 2 * sizeof(uint64_t); }
+
+__global__ void __launch_bounds__(256, 4) ref_pass_b_staged_kernel(RefIterArgs a) {
+    extern __shared__ __align__(128) unsigned char gb_raw[];
+    float* box = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(gb_raw) + 127) & ~uintptr_t(127));
+    uint64_t* full = reinterpret_cast<uint64_t*>(box + 2 * 3 * kGBPlane);
+    __shared__ unsigned long long red[32];
+    __shared__ bool last;
+    __shared__ CellBoxSets cb;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(full, 1);
+        mbar_init(full + 1, 1);
+        mbar_fence_init();
+        for (int k = 0; k < 3; ++k) cellbox_clear(cb, k);
+    }
+    __syncthreads();
+    const int dst = a.iter & 1;  // the velocity buffer pass A just wrote
+    unsigned g = 0;       // slices reduced by this block (cell-box set g % 3)
+    unsigned nbox = 0;    // boxes issued by this block (buffer nbox & 1, parity (nbox >> 1) & 1)
+    bool failed = false, wait_failed = false;
+    for (int t = blockIdx.x; t < a.ntiles_b && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_b[t];
+        if (a.stop[tl.x]) continue;  // uniform over the block
+        const Pair P = a.pairs[tl.x];
+        const int x = tl.y + (int)(tid & 31), y = tl.z + (int)(tid >> 5);
+        const int X = P.X, Y = P.Y, Z = P.Z, Xp = P.Xp, XYp = P.Xp * P.Y;
+        const bool col = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
+        const long long NT = a.NT;
+        const float* __restrict__ V[3] = {a.v_n + P.off, a.v_n + NT + P.off, a.v_n + 2 * NT + P.off};
+        float* Q[3] = {a.psi + P.off, a.psi + NT + P.off, a.psi + 2 * NT + P.off};
+        const CUtensorMap* mv = a.tmaps + (long long)tl.x * TM_COUNT + TM_PB_V0 + dst;
+        const int z0 = max(tl.w, 1), z1 = min(tl.w + a.depth_b, Z - 1);
+        unsigned long long best = 0ull;
+        // the slice being prepared: positions, cell, and whether its box was issued (and where)
+        float px = 0.f, py = 0.f, pz = 0.f;
+        Cell32 cl{};
+        int i = x + Xp * y + XYp * z0;
+        if (col && z0 < z1) {
+            px = Q[0][i];
+            py = Q[1][i];
+            pz = Q[2][i];
+            cl = locate32(X, Y, Z, Xp, px, py, pz);
+        }
+        // box of a reduced slice: issue it when it fits (uniform decision); returns the box
+        // origin in o[] and whether it was issued
+        auto plan = [&](unsigned set, int zz, int o[3]) -> bool {
+            int lo[3], hi[3];
+            if (!cellbox_read(cb, (int)set, lo, hi)) return false;
+            o[0] = lo[0] & ~3;
+            o[1] = lo[1];
+            o[2] = lo[2];
+            const bool fits = hi[0] + 1 - o[0] < kGBX && hi[1] + 1 - o[1] < kGBY && hi[2] + 1 - o[2] < kGBZ;
+            if (fits && tid == 0) {
+                uint64_t* bar = full + (nbox & 1);
+                mbar_arrive_expect_tx(bar, kGBBytes);
+                tma_load_4d(box + (nbox & 1) * 3 * kGBPlane, mv, o[0], o[1], o[2], 0, bar);
+            }
+            return fits;
+        };
+        // prologue: the first slice's box (a fresh set: the previous tile's last one may
+        // still be read by slower threads)
+        ++g;
+        cellbox_add(cb, (int)(g % 3), col && z0 < z1, cl.gx, cl.gy, cl.gz);
+        if (__syncthreads_or(wait_failed)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) cellbox_clear(cb, (int)((g - 1) % 3));
+        int org[3] = {0, 0, 0};
+        bool staged = plan(g % 3, z0, org);
+        unsigned mybox = nbox;
+        if (staged) ++nbox;
+        for (int z = z0; z < z1; ++z, i += XYp) {
+            // this slice's state
+            const float cx = px, cy = py, cz = pz;
+            const Cell32 c = cl;
+            const bool cur_staged = staged;
+            const unsigned cur_box = mybox;
+            const int o0 = org[0], o1 = org[1], o2 = org[2];
+            // the next slice's positions and cell, its box reduced and issued
+            const bool nact = col && z + 1 < z1;
+            if (nact) {
+                px = Q[0][i + XYp];
+                py = Q[1][i + XYp];
+                pz = Q[2][i + XYp];
+                cl = locate32(X, Y, Z, Xp, px, py, pz);
+            }
+            ++g;
+            cellbox_add(cb, (int)(g % 3), nact, cl.gx, cl.gy, cl.gz);
+            // every thread is past slice z - 1 (its buffer is free), the next box is
+            // reduced, and the block agrees on whether a wait gave up
+            if (__syncthreads_or(wait_failed)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0) cellbox_clear(cb, (int)((g - 1) % 3));
+            staged = plan(g % 3, z + 1, org);
+            mybox = nbox;
+            if (staged) ++nbox;
+            if (!col) continue;
+            float u[3];
+            const bool inside = c.gx + 1 < X && c.gy + 1 < Y && c.gz + 1 < Z;
+            if (cur_staged && inside) {
+                if (!mbar_wait_bounded(full + (cur_box & 1), (cur_box >> 1) & 1)) wait_failed = true;
+                const float* b0 = box + (cur_box & 1) * 3 * kGBPlane + ((c.gz - o2) * kGBY + (c.gy - o1)) * kGBX +
+                                  (c.gx - o0);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float* f = b0 + k * kGBPlane;
+                    constexpr int SX = 1, SY = kGBX, SZ = kGBX * kGBY;
+                    u[k] = a.alpha * trilerp(f[SX + SY + SZ], f[SX + SY], f[SX + SZ], f[SX], f[SY + SZ], f[SY],
+                                             f[SZ], f[0], c.a, c.b, c.c);
+                }
+            } else {
+                if (cur_staged && !mbar_wait_bounded(full + (cur_box & 1), (cur_box >> 1) & 1)) wait_failed = true;
+#pragma unroll
+                for (int k = 0; k < 3; ++k) u[k] = a.alpha * tri_checked32(V[k], X, Y, Z, Xp, XYp, c);
+            }
+            Q[0][i] = cx + u[0];
+            Q[1][i] = cy + u[1];
+            Q[2][i] = cz + u[2];
+            const float nrm = norm3_rd(u[0], u[1], u[2]);
+            if (nrm == nrm) {  // NaN norms never win, as in the reference's '>' test
+                const unsigned long long k = norm_key(nrm, i);
+                best = k > best ? k : best;
+            }
+        }
+        if (failed) break;
+        const unsigned long long bm = block_max_u64(best, red);
+        if (tid == 0 && bm) atomicMax(a.keys + tl.x, bm);
+    }
+    if (failed) {
+        if (tid == 0) {
+            for (unsigned n = (nbox > 2u ? nbox - 2u : 0u); n < nbox; ++n)
+                mbar_wait_bounded(full + (n & 1), (n >> 1) & 1);
+            atomicOr(a.err, kErrTmaTimeout);
+        }
+        return;  // the iteration's record is left to the blocks that finished
+    }
+
+    // the last block to finish records this iteration and decides convergence
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int p = tid; p < a.npairs; p += blockDim.x) {
+        if (a.stop[p]) continue;
+        const unsigned long long k = atomicExch(a.keys + p, 0ull);
+        a.trace[(long long)(a.iter - 1) * a.npairs + p] = k;
+        const float mx = __uint_as_float((unsigned)(k >> 32));
+        if (mx <= a.max_update_norm) a.stop[p] = a.iter;
+    }
+    if (tid == 0) *a.counter = 0u;
+}
+
 }  // namespace frg

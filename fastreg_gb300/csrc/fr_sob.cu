@@ -29,6 +29,7 @@ void gaussian_taps(float sigma, int width, float* taps) {
 // were outside [0, dim-1] (their derivative along that axis is 0).
 struct SobCell {
     long long base;
+    int gx, gy, gz;
     float a, b, c;
     bool in_x, in_y, in_z;
 };
@@ -47,6 +48,9 @@ __device__ __forceinline__ SobCell sob_locate(const Pair& P, float px, float py,
     s.in_x = px >= 0.f && px <= (float)(P.X - 1);
     s.in_y = py >= 0.f && py <= (float)(P.Y - 1);
     s.in_z = pz >= 0.f && pz <= (float)(P.Z - 1);
+    s.gx = gx;
+    s.gy = gy;
+    s.gz = gz;
     s.base = lin(P, gx, gy, gz);
     return s;
 }
@@ -663,6 +667,164 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
     if (threadIdx.x == 0) *a.counter = 0u;
 }
 
+// The compositional update with the gathered neighbourhood of m staged in shared memory,
+// as ref_pass_b_staged_kernel does for v: per slice the block reduces its cells' bounding
+// box and, when it fits kGBX x kGBY x kGBZ, one tensor copy brings that box of m's three
+// components into one of two buffers while the previous slice is gathered.  The sobolev
+// cell's floor is clamped to dim - 2, so every corner is inside the grid; slices whose
+// cells do not fit gather from global memory as sob_pass_b_kernel does, with the same
+// arithmetic.  Waits are bounded as in ref_pass_b_staged_kernel.
+__global__ void __launch_bounds__(256, 4) sob_pass_b_staged_kernel(SobIterArgs a) {
+    constexpr int kPlane = kGBX * kGBY * kGBZ;
+    constexpr unsigned kBytes = sizeof(float) * 3 * kPlane;
+    extern __shared__ __align__(128) unsigned char sb_raw[];
+    float* box = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(sb_raw) + 127) & ~uintptr_t(127));
+    uint64_t* full = reinterpret_cast<uint64_t*>(box + 2 * 3 * kPlane);
+    __shared__ unsigned long long red[32];
+    __shared__ bool last;
+    __shared__ CellBoxSets cb;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(full, 1);
+        mbar_init(full + 1, 1);
+        mbar_fence_init();
+        for (int k = 0; k < 3; ++k) cellbox_clear(cb, k);
+    }
+    __syncthreads();
+    unsigned g = 0, nbox = 0;
+    bool failed = false, wait_failed = false;
+    for (int t = blockIdx.x; t < a.ntiles_b && !failed; t += gridDim.x) {
+        const Tile tl = a.tiles_b[t];
+        if (a.stop[tl.x]) continue;
+        const Pair P = a.pairs[tl.x];
+        const int x = tl.y + (int)(tid & 31), y = tl.z + (int)(tid >> 5);
+        const bool col = x < P.X && y < P.Y;
+        const long long NT = a.NT;
+        const int X = P.Xp, XY = P.Xp * P.Y;  // strides of the packed arrays
+        float* phi[3] = {a.phi + P.off, a.phi + NT + P.off, a.phi + 2 * NT + P.off};
+        const float* __restrict__ mc[3] = {a.m + P.off, a.m + NT + P.off, a.m + 2 * NT + P.off};
+        const CUtensorMap* mm = a.tmaps + (long long)tl.x * TM_COUNT + TM_SB_M;
+        const int z0 = tl.w, z1 = min(tl.w + a.depth_b, P.Z);
+        unsigned long long best = 0ull;
+        int i = x + X * y + XY * z0;
+        float px = 0.f, py = 0.f, pz = 0.f;
+        SobCell cl{};
+        if (col) {
+            px = phi[0][i];
+            py = phi[1][i];
+            pz = phi[2][i];
+            cl = sob_locate(P, px, py, pz);
+        }
+        auto plan = [&](unsigned set, int o[3]) -> bool {
+            int lo[3], hi[3];
+            if (!cellbox_read(cb, (int)set, lo, hi)) return false;
+            o[0] = lo[0] & ~3;
+            o[1] = lo[1];
+            o[2] = lo[2];
+            const bool fits = hi[0] + 1 - o[0] < kGBX && hi[1] + 1 - o[1] < kGBY && hi[2] + 1 - o[2] < kGBZ;
+            if (fits && tid == 0) {
+                uint64_t* bar = full + (nbox & 1);
+                mbar_arrive_expect_tx(bar, kBytes);
+                tma_load_4d(box + (nbox & 1) * 3 * kPlane, mm, o[0], o[1], o[2], 0, bar);
+            }
+            return fits;
+        };
+        ++g;
+        cellbox_add(cb, (int)(g % 3), col, cl.gx, cl.gy, cl.gz);
+        if (__syncthreads_or(wait_failed)) {
+            failed = true;
+            break;
+        }
+        if (tid == 0) cellbox_clear(cb, (int)((g - 1) % 3));
+        int org[3] = {0, 0, 0};
+        bool staged = plan(g % 3, org);
+        unsigned mybox = nbox;
+        if (staged) ++nbox;
+        for (int z = z0; z < z1; ++z, i += XY) {
+            const float cx = px, cy = py, cz = pz;
+            const SobCell c = cl;
+            const bool cur_staged = staged;
+            const unsigned cur_box = mybox;
+            const int o0 = org[0], o1 = org[1], o2 = org[2];
+            const bool nact = col && z + 1 < z1;
+            if (nact) {
+                px = phi[0][i + XY];
+                py = phi[1][i + XY];
+                pz = phi[2][i + XY];
+                cl = sob_locate(P, px, py, pz);
+            }
+            ++g;
+            cellbox_add(cb, (int)(g % 3), nact, cl.gx, cl.gy, cl.gz);
+            if (__syncthreads_or(wait_failed)) {
+                failed = true;
+                break;
+            }
+            if (tid == 0) cellbox_clear(cb, (int)((g - 1) % 3));
+            staged = plan(g % 3, org);
+            mybox = nbox;
+            if (staged) ++nbox;
+            if (!col) continue;
+            float u[3];
+            if (cur_staged) {
+                if (!mbar_wait_bounded(full + (cur_box & 1), (cur_box >> 1) & 1)) wait_failed = true;
+                const float* b0 =
+                    box + (cur_box & 1) * 3 * kPlane + ((c.gz - o2) * kGBY + (c.gy - o1)) * kGBX + (c.gx - o0);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float* f = b0 + k * kPlane;
+                    constexpr int SX = 1, SY = kGBX, SZ = kGBX * kGBY;
+                    u[k] = lerpf_(lerpf_(lerpf_(f[SX + SY + SZ], f[SX + SY], c.c), lerpf_(f[SX + SZ], f[SX], c.c), c.b),
+                                  lerpf_(lerpf_(f[SY + SZ], f[SY], c.c), lerpf_(f[SZ], f[0], c.c), c.b), c.a);
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const float* __restrict__ F = mc[k];
+                    const int b = (int)c.base;
+                    u[k] = lerpf_(lerpf_(lerpf_(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), c.c),
+                                         lerpf_(__ldg(F + b + 1 + XY), __ldg(F + b + 1), c.c), c.b),
+                                  lerpf_(lerpf_(__ldg(F + b + X + XY), __ldg(F + b + X), c.c),
+                                         lerpf_(__ldg(F + b + XY), __ldg(F + b), c.c), c.b),
+                                  c.a);
+                }
+            }
+            phi[0][i] = cx + u[0];
+            phi[1][i] = cy + u[1];
+            phi[2][i] = cz + u[2];
+            const float nrm = norm3_rd(u[0], u[1], u[2]);
+            if (nrm == nrm) {
+                const unsigned long long k = norm_key(nrm, i);
+                best = k > best ? k : best;
+            }
+        }
+        if (failed) break;
+        const unsigned long long bm = block_max_u64(best, red);
+        if (tid == 0 && bm) atomicMax(a.keys + tl.x, bm);
+    }
+    if (failed) {
+        if (tid == 0) {
+            for (unsigned n = (nbox > 2u ? nbox - 2u : 0u); n < nbox; ++n)
+                mbar_wait_bounded(full + (n & 1), (n >> 1) & 1);
+            atomicOr(a.err, kErrTmaTimeout);
+        }
+        return;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) last = (atomicAdd(a.counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    for (int p = tid; p < a.npairs; p += blockDim.x) {
+        if (a.stop[p]) continue;
+        const unsigned long long k = atomicExch(a.keys + p, 0ull);
+        a.trace[(long long)(a.iter - 1) * a.npairs + p] = k;
+        const float mx = __uint_as_float((unsigned)(k >> 32));
+        if (mx <= a.max_update_norm) a.stop[p] = a.iter;
+    }
+    if (tid == 0) *a.counter = 0u;
+}
+
 cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, const int* variants, cudaStream_t s,
                             cudaEvent_t* ev) {
     if (ev) cudaEventRecord(ev[0], s);
@@ -676,7 +838,10 @@ cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, const int* v
         cudaLaunchKernel(sob_smooth3_fn(a.radius, variants[1]), dim3(grids[1]), dim3(256), args, 0, s);
     }
     if (ev) cudaEventRecord(ev[2], s);
-    sob_pass_b_kernel<<<grids[2], 256, 0, s>>>(a);
+    if (variants[2])
+        sob_pass_b_staged_kernel<<<grids[2], 256, gather_staged_smem_bytes(), s>>>(a);
+    else
+        sob_pass_b_kernel<<<grids[2], 256, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);
     return cudaGetLastError();
 }

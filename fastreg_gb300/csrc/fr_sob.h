@@ -72,8 +72,9 @@ inline void sob_smooth_box(int R, int* wx, int* rows) {
     *rows = kSobTileY + 2 * R;
 }
 __global__ void sob_pass_b_kernel(SobIterArgs a);
+__global__ void sob_pass_b_staged_kernel(SobIterArgs a);
 
-// grids: {grad, smooth, pass_b}; variants: staging of {grad, smooth} (1: TMA); with `ev`
+// grids: {grad, smooth, pass_b}; variants: staging of {grad, smooth, pass_b} (1: TMA); with `ev`
 // (4 events) each launch is bracketed
 cudaError_t launch_sob_iter(const SobIterArgs& a, const int* grids, const int* variants, cudaStream_t s,
                             cudaEvent_t* ev = nullptr);

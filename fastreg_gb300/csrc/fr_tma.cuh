@@ -96,4 +96,46 @@ struct SliceRing {
 // Codes of the device error word (RefIterArgs::err, SobIterArgs::err).
 constexpr unsigned kErrTmaTimeout = 1u;
 
+// ---- a slice's source neighbourhood: the bounding box of the block's trilinear cells ----
+// The gathers of the update kernels read, per voxel, the eight corners of the cell that
+// holds its sample position.  The map is smooth, so the cells of one slice of a 32 x 8
+// tile lie in a small box of the gathered field; the box is copied into shared memory by
+// one tensor copy and the corners are read from there.  The box of slice j is reduced
+// over the block into set j % 3 of a CellBoxSets (min of gx, gy, gz and of their
+// negations): redux.sync per warp, one shared-memory atomicMin per warp and value, and
+// one block barrier, after which every thread reads it.  Three sets rotate so that one
+// barrier per slice suffices: set j % 3 is cleared by thread 0 after barrier j + 1 (all
+// threads have read it) and refilled after barrier j + 2.
+struct CellBoxSets {
+    int v[3][6];
+};
+constexpr int kCellBoxEmpty = 0x7fffffff;
+
+__device__ __forceinline__ void cellbox_clear(CellBoxSets& s, int set) {
+    for (int k = 0; k < 6; ++k) s.v[set][k] = kCellBoxEmpty;
+}
+
+// every thread of the block calls it; act: this thread has a cell in the slice
+__device__ __forceinline__ void cellbox_add(CellBoxSets& s, int set, bool act, int gx, int gy, int gz) {
+    const unsigned full = 0xffffffffu;
+    int r[6] = {act ? gx : kCellBoxEmpty,  act ? gy : kCellBoxEmpty,  act ? gz : kCellBoxEmpty,
+                act ? -gx : kCellBoxEmpty, act ? -gy : kCellBoxEmpty, act ? -gz : kCellBoxEmpty};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) r[k] = __reduce_min_sync(full, r[k]);
+    if ((threadIdx.x & 31) == 0 && r[0] != kCellBoxEmpty)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) atomicMin(&s.v[set][k], r[k]);
+}
+
+// after the barrier: the box of set `set`, cells' floor corners gx in [lo[0], hi[0]] etc.;
+// false if the slice had no cell
+__device__ __forceinline__ bool cellbox_read(const CellBoxSets& s, int set, int lo[3], int hi[3]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        lo[k] = s.v[set][k];
+        hi[k] = -s.v[set][3 + k];
+    }
+    return lo[0] != kCellBoxEmpty;
+}
+
 }  // namespace frg

@@ -191,7 +191,11 @@ int fr_interpolate_field(const float *d_field, const float *d_pos, const int dim
  * regulariser weighted by lambda (W_REG).  Writes J to *loss and, when d_grad_v0 is not
  * NULL, dJ/dv0 (3 planes, device) and dJ/dlambda to *grad_lambda, by hand-written
  * adjoint kernels with the forward states checkpointed every `checkpoint_every`
- * iterations.  d_T, d_S: target and source (N floats each).  Synchronises `stream`. */
+ * iterations.  d_T, d_S: target and source (N floats each).  Synchronises `stream`.
+ * Its device workspace (checkpoints and adjoint fields, about 3 N floats x (2 (iters /
+ * checkpoint_every + 1) + 2 checkpoint_every + 8)) is kept per device after the call and
+ * reused by later calls of the same or a smaller size; a call made while another host
+ * thread's call holds it allocates a private one. */
 int fr_sobolev_loss_grad(const float *d_T, const float *d_S, const int dims[3], const float *d_v0, float lambda,
                          int iters, int checkpoint_every, float damping, float step, float smooth_sigma,
                          int smooth_width, double *loss, float *d_grad_v0, double *grad_lambda, void *stream);
