@@ -914,7 +914,7 @@ int autotune(fr_handle* h, cudaStream_t s) {
             if (occ > 1) bps.push_back(occ - 1);
             if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
             bps.push_back(-1);  // one block per tile
-            for (int depth : {1, 2, 4, 8, 12, 16, 24, 32, 48})
+            for (int depth : {1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96})
                 for (int b : bps) cand.push_back(Shape{depth, b, v});
         }
         // two passes over the candidates, each candidate's faster time kept (less noise)

@@ -240,7 +240,9 @@ __global__ void __launch_bounds__(256) warp_kernel(const float* __restrict__ pos
 // Four consecutive voxels per thread (32-bit indices): 16-byte loads of the three
 // position planes, issued one grid-stride item ahead so that they are in flight with the
 // current item's 32 corner and 4 label loads; a 16-byte store of the intensities and an
-// 8-byte store of the labels.  The caller guarantees N = X*Y*Z a multiple of 4 below 2^31
+// 8-byte store of the labels.  Positions and outputs are touched once and go through the
+// cache as streaming (evict-first) accesses, leaving L1 and L2 to the corner gathers,
+// which neighbouring voxels share.  The caller guarantees N = X*Y*Z a multiple of 4 below 2^31
 // and 16-byte (pos, out) / 8-byte (out_lab) aligned buffers; per voxel the arithmetic is
 // warp_kernel's (corners past the last voxel, of weight 0, clamped as tri_unchecked32
 // does).
@@ -252,17 +254,17 @@ __global__ void __launch_bounds__(256) warp4_kernel(const float* __restrict__ po
     const int stride = gridDim.x * blockDim.x;
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     float4 npx = make_float4(0.f, 0.f, 0.f, 0.f), npy = npx, npz = npx;
-    if (t < N4) {
-        npx = __ldg(p4 + t);
-        npy = __ldg(p4 + N4 + t);
-        npz = __ldg(p4 + 2 * N4 + t);
+    if (t < N4) {  // positions are read once: streaming loads, evicted first
+        npx = __ldcs(p4 + t);
+        npy = __ldcs(p4 + N4 + t);
+        npz = __ldcs(p4 + 2 * N4 + t);
     }
     for (; t < N4; t += stride) {
         const float4 px = npx, py = npy, pz = npz;
         if (t + stride < N4) {  // the next item's positions load while this one's corners do
-            npx = __ldg(p4 + t + stride);
-            npy = __ldg(p4 + N4 + t + stride);
-            npz = __ldg(p4 + 2 * N4 + t + stride);
+            npx = __ldcs(p4 + t + stride);
+            npy = __ldcs(p4 + N4 + t + stride);
+            npz = __ldcs(p4 + 2 * N4 + t + stride);
         }
         const float xs[4] = {px.x, px.y, px.z, px.w}, ys[4] = {py.x, py.y, py.z, py.w},
                     zs[4] = {pz.x, pz.y, pz.z, pz.w};
@@ -284,14 +286,14 @@ __global__ void __launch_bounds__(256) warp4_kernel(const float* __restrict__ po
         for (int k = 0; k < 4; ++k)
             r[k] = trilerp(f[k][0], f[k][1], f[k][2], f[k][3], f[k][4], f[k][5], f[k][6], f[k][7], cl[k].a, cl[k].b,
                            cl[k].c);
-        reinterpret_cast<float4*>(out)[t] = make_float4(r[0], r[1], r[2], r[3]);
+        __stcs(reinterpret_cast<float4*>(out) + t, make_float4(r[0], r[1], r[2], r[3]));  // written once
         if (out_lab) {
             short4 l;
             l.x = lb[0];
             l.y = lb[1];
             l.z = lb[2];
             l.w = lb[3];
-            reinterpret_cast<short4*>(out_lab)[t] = l;
+            __stcs(reinterpret_cast<short4*>(out_lab) + t, l);
         }
     }
 }

@@ -369,11 +369,30 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
             const float* src = &G[k % NB][0][0][0];
             float* dst = &Gx[k & 1][0][0][0];
+            // rows ty + 8 j, two at a time as one packed pair (per lane the same fused
+            // multiply-adds as one row at a time)
 #pragma unroll
-            for (int j = 0; j < RW; ++j) {
-                const int rr = ty + kSobTileY * j;  // row rr of the 3 H staged rows
-                if (rr < 3 * H) {
-                    const float* row = src + rr * WS;
+            for (int j = 0; j < RW; j += 2) {
+                const int r0 = ty + kSobTileY * j, r1 = r0 + kSobTileY;  // rows of the 3 H staged rows
+                if (j + 1 < RW && r1 < 3 * H) {
+                    const float *w0 = src + r0 * WS, *w1 = src + r1 * WS;
+                    float2 acc = make_float2(0.f, 0.f);
+                    if (!xedge) {
+#pragma unroll
+                        for (int q = 0; q < K; ++q)
+                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]),
+                                             make_float2(w0[HX - R + tx + q], w1[HX - R + tx + q]), acc);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) {
+                            const int xi = min(max(x0 - R + tx + q, 0), X - 1) - (x0 - HX);
+                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]), make_float2(w0[xi], w1[xi]), acc);
+                        }
+                    }
+                    dst[r0 * kTileX + tx] = acc.x;
+                    dst[r1 * kTileX + tx] = acc.y;
+                } else if (r0 < 3 * H) {
+                    const float* row = src + r0 * WS;
                     float acc = 0.f;
                     if (!xedge) {
 #pragma unroll
@@ -385,7 +404,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
                             acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
                         }
                     }
-                    dst[rr * kTileX + tx] = acc;
+                    dst[r0 * kTileX + tx] = acc;
                 }
             }
         };
@@ -398,7 +417,8 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) mv[c] = m[c][col + XY * zt0];
 
-        float ring[K][3];
+        float2 ring01[K];  // the z ring of the y-pass results: components 0 and 1 packed, 2
+        float ring2[K];
         __syncthreads();  // the previous tile is done with G and Gx
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
@@ -417,25 +437,39 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
             if (k + 1 < nsl) x_pass(k + 1);
             // y pass of slice k for this thread's column, pushed into the z ring
 #pragma unroll
-            for (int q = 0; q < K - 1; ++q)
+            for (int q = 0; q < K - 1; ++q) {
+                ring01[q] = ring01[q + 1];
+                ring2[q] = ring2[q + 1];
+            }
+            {  // components 0 and 1 as one packed pair: per lane the same fused multiply-adds
+                float2 acc01 = make_float2(0.f, 0.f);
+                float acc2 = 0.f;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) ring[q][c] = ring[q + 1][c];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                float acc = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], Gx[k & 1][c][ty + q][tx], acc);
-                ring[K - 1][c] = acc;
+                for (int q = 0; q < K; ++q) {
+                    const float w = a.taps[q];
+                    acc01 = __ffma2_rn(make_float2(w, w),
+                                       make_float2(Gx[k & 1][0][ty + q][tx], Gx[k & 1][1][ty + q][tx]), acc01);
+                    acc2 = fmaf(w, Gx[k & 1][2][ty + q][tx], acc2);
+                }
+                ring01[K - 1] = acc01;
+                ring2[K - 1] = acc2;
             }
             // z pass and momentum for slice zt0 + k - 2R once the ring holds its 2R + 1 slices
             const int zo = zt0 - 2 * R + k;
             if (k >= 2 * R && inside) {
                 const int i = col + XY * zo;
+                float2 acc01 = make_float2(0.f, 0.f);
+                float acc2 = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) {
+                    const float w = a.taps[q];
+                    acc01 = __ffma2_rn(make_float2(w, w), ring01[q], acc01);
+                    acc2 = fmaf(w, ring2[q], acc2);
+                }
+                const float accs[3] = {acc01.x, acc01.y, acc2};
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], ring[q][c], acc);
+                    const float acc = accs[c];
                     const float mo = mv[c];
                     if (zo + 1 < zt1) mv[c] = m[c][i + XY];  // the next output slice's momentum
                     m[c][i] = a.damping * mo - a.step * acc;
@@ -500,13 +534,35 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
             const float* src = &G[Ring::slot(nbase + (unsigned)k)][0];
             float* dst = &Gx[k & 1][0][0][0];
+            // staged row rr holds the clamped row of component c: rows two at a time as one
+            // packed pair, as in sob_smooth3_kernel
+            auto row_of = [&](int rr) {
+                const int c = rr / H, r = rr - c * H;
+                const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);  // the clamped row
+                return src + (c * H + rs) * WS;
+            };
 #pragma unroll
-            for (int j = 0; j < RW; ++j) {
-                const int rr = ty + kSobTileY * j;  // row rr of the 3 H staged rows
-                if (rr < 3 * H) {
-                    const int c = rr / H, r = rr - c * H;
-                    const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);  // the clamped row
-                    const float* row = src + (c * H + rs) * WS;
+            for (int j = 0; j < RW; j += 2) {
+                const int r0 = ty + kSobTileY * j, r1 = r0 + kSobTileY;
+                if (j + 1 < RW && r1 < 3 * H) {
+                    const float *w0 = row_of(r0), *w1 = row_of(r1);
+                    float2 acc = make_float2(0.f, 0.f);
+                    if (!xedge) {
+#pragma unroll
+                        for (int q = 0; q < K; ++q)
+                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]),
+                                             make_float2(w0[HX - R + tx + q], w1[HX - R + tx + q]), acc);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < K; ++q) {
+                            const int xi = min(max(x0 - R + tx + q, 0), X - 1) - (x0 - HX);
+                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]), make_float2(w0[xi], w1[xi]), acc);
+                        }
+                    }
+                    dst[r0 * kTileX + tx] = acc.x;
+                    dst[r1 * kTileX + tx] = acc.y;
+                } else if (r0 < 3 * H) {
+                    const float* row = row_of(r0);
                     float acc = 0.f;
                     if (!xedge) {
 #pragma unroll
@@ -518,7 +574,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
                             acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
                         }
                     }
-                    dst[rr * kTileX + tx] = acc;
+                    dst[r0 * kTileX + tx] = acc;
                 }
             }
         };
@@ -533,7 +589,8 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) mv[c] = m[c][col + XY * zt0];
 
-        float ring[K][3];
+        float2 ring01[K];  // the z ring of the y-pass results: components 0 and 1 packed, 2
+        float ring2[K];
         __syncthreads();  // the previous tile is done with G and Gx
         if (tid == 0) {
             tma_prefetch_map(mg);
@@ -555,24 +612,38 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
             if (tid == 0 && k + NT < nsl) issue(k + NT);  // into slice k's buffer
             if (k + 1 < nsl) x_pass(k + 1);
 #pragma unroll
-            for (int q = 0; q < K - 1; ++q)
+            for (int q = 0; q < K - 1; ++q) {
+                ring01[q] = ring01[q + 1];
+                ring2[q] = ring2[q + 1];
+            }
+            {  // components 0 and 1 as one packed pair: per lane the same fused multiply-adds
+                float2 acc01 = make_float2(0.f, 0.f);
+                float acc2 = 0.f;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) ring[q][c] = ring[q + 1][c];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                float acc = 0.f;
-#pragma unroll
-                for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], Gx[k & 1][c][ty + q][tx], acc);
-                ring[K - 1][c] = acc;
+                for (int q = 0; q < K; ++q) {
+                    const float w = a.taps[q];
+                    acc01 = __ffma2_rn(make_float2(w, w),
+                                       make_float2(Gx[k & 1][0][ty + q][tx], Gx[k & 1][1][ty + q][tx]), acc01);
+                    acc2 = fmaf(w, Gx[k & 1][2][ty + q][tx], acc2);
+                }
+                ring01[K - 1] = acc01;
+                ring2[K - 1] = acc2;
             }
             const int zo = zt0 - 2 * R + k;
             if (k >= 2 * R && inside) {
                 const int i = col + XY * zo;
+                float2 acc01 = make_float2(0.f, 0.f);
+                float acc2 = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) {
+                    const float w = a.taps[q];
+                    acc01 = __ffma2_rn(make_float2(w, w), ring01[q], acc01);
+                    acc2 = fmaf(w, ring2[q], acc2);
+                }
+                const float accs[3] = {acc01.x, acc01.y, acc2};
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    float acc = 0.f;
-#pragma unroll
-                    for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], ring[q][c], acc);
+                    const float acc = accs[c];
                     const float mo = mv[c];
                     if (zo + 1 < zt1) mv[c] = m[c][i + XY];
                     m[c][i] = a.damping * mo - a.step * acc;

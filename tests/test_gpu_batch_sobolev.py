@@ -108,7 +108,7 @@ def test_autotuned_shapes_do_not_change_results(cuda, solver):
         fr.register_batch(bufs)
         fields.append([fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy() for k in range(len(dims_list))])
         shapes = fr.tile_shapes()
-        assert all(d in (1, 2, 4, 8, 12, 16, 24, 32, 48) and (b >= 1 or b == -1) for d, b in shapes), shapes
+        assert all(d in (1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96) and (b >= 1 or b == -1) for d, b in shapes), shapes
         if not tune:
             default = (16, 24, 24) if solver == "reference" else (12, 32, 8)
             assert tuple(d for d, _ in shapes) == default, shapes
