@@ -118,6 +118,7 @@ SIGNATURES = [
                                   C.c_void_p]),
     ("fr_stats_noalloc", C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_int),
                                    C.c_int, C.c_float, C.POINTER(fr_stats), C.c_void_p]),
+    ("fr_selftest_wait_limit", C.c_int, [C.POINTER(C.c_double), C.c_void_p]),
     ("fr_last_error", C.c_char_p, [C.c_void_p]),
     ("fr_status_string", C.c_char_p, [C.c_int]),
     ("fr_abi_version", C.c_int, []),

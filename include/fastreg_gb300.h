@@ -232,6 +232,14 @@ int fr_warp_adjoint(const float *d_pos, const float *d_img, const float *d_wbar,
 int fr_stats_noalloc(const float *d_T, const int16_t *d_labT, const float *d_warped_S, const int16_t *d_warped_labS,
                      const float *d_psi, const int dims[3], int no_labels, float w_reg, fr_stats *out, void *stream);
 
+/* Self-test of the TMA-staged kernels' failure path (no counterpart in the reference): one
+ * block waits, with the kernels' bounded wait, on an mbarrier armed for bytes that no copy
+ * delivers, gives up after the limit (about 2^31 clock cycles, a second), and sets the
+ * device error word as a staged kernel would.  Returns FR_OK when the wait gave up as
+ * designed (*seconds: the call's wall time), FR_ERR_STATE otherwise; the GPU stays usable
+ * either way.  Synchronises `stream`. */
+int fr_selftest_wait_limit(double *seconds, void *stream);
+
 const char *fr_last_error(const fr_handle *h);
 const char *fr_status_string(int status);
 int fr_abi_version(void);
