@@ -139,6 +139,38 @@ __device__ __forceinline__ float trilerp(float f111, float f110, float f101, flo
                   lerpf_(lerpf_(f011, f010, c), lerpf_(f001, f000, c), b), a);
 }
 
+// Two lerps as one packed FP32 pair: per lane exactly lerpf_(v0, v1, t) (both fused
+// multiply-adds of a lane are the lane's own, rounded once each).  nt = -t, passed in so
+// that a cell's negated weights are formed once.
+__device__ __forceinline__ float2 lerp2_(float2 v0, float2 v1, float2 t, float2 nt) {
+    return __ffma2_rn(t, v0, __ffma2_rn(nt, v1, v1));
+}
+
+// two trilerps as one packed pair, each lane with its own corner values and weights
+__device__ __forceinline__ float2 trilerp2w(float2 f111, float2 f110, float2 f101, float2 f100, float2 f011,
+                                            float2 f010, float2 f001, float2 f000, float2 ta, float2 tb, float2 tc) {
+    const float2 na = make_float2(-ta.x, -ta.y), nb = make_float2(-tb.x, -tb.y), nc = make_float2(-tc.x, -tc.y);
+    return lerp2_(lerp2_(lerp2_(f111, f110, tc, nc), lerp2_(f101, f100, tc, nc), tb, nb),
+                  lerp2_(lerp2_(f011, f010, tc, nc), lerp2_(f001, f000, tc, nc), tb, nb), ta, na);
+}
+
+// trilerp of two fields at one cell as one packed pair (lane 0: field 0, lane 1: field 1)
+__device__ __forceinline__ float2 trilerp2(float2 f111, float2 f110, float2 f101, float2 f100, float2 f011,
+                                           float2 f010, float2 f001, float2 f000, float a, float b, float c) {
+    return trilerp2w(f111, f110, f101, f100, f011, f010, f001, f000, make_float2(a, a), make_float2(b, b),
+                     make_float2(c, c));
+}
+
+// trilerp of three fields' corners f[k][0..7] (order 111, 110, 101, 100, 011, 010, 001, 000)
+// at one cell: fields 0 and 1 as one packed pair, field 2 alone; per field exactly trilerp
+__device__ __forceinline__ void trilerp3(const float f[3][8], float a, float b, float c, float out[3]) {
+    auto p = [&](int q) { return make_float2(f[0][q], f[1][q]); };
+    const float2 r = trilerp2(p(0), p(1), p(2), p(3), p(4), p(5), p(6), p(7), a, b, c);
+    out[0] = r.x;
+    out[1] = r.y;
+    out[2] = trilerp(f[2][0], f[2][1], f[2][2], f[2][3], f[2][4], f[2][5], f[2][6], f[2][7], a, b, c);
+}
+
 // tri_unchecked with 32-bit indices: corners past the last voxel (only possible when
 // the cell touches the end of the array) are clamped on a slow path.  X, XY, N are the
 // strides and extent of the array (pitched for the packed arrays).
@@ -152,6 +184,44 @@ __device__ __forceinline__ float tri_unchecked32(const float* __restrict__ F, in
     return trilerp(__ldg(F + min(b + 1 + X + XY, last)), __ldg(F + min(b + 1 + X, last)),
                    __ldg(F + min(b + 1 + XY, last)), __ldg(F + min(b + 1, last)), __ldg(F + min(b + X + XY, last)),
                    __ldg(F + min(b + X, last)), __ldg(F + min(b + XY, last)), __ldg(F + b), cl.a, cl.b, cl.c);
+}
+
+// The three components of a vector field (planes F0, F1, F2) at one cell with
+// tri_checked32's addressing; components 0 and 1 interpolated as one packed pair.
+__device__ __forceinline__ void tri_checked32_3(const float* __restrict__ F0, const float* __restrict__ F1,
+                                                const float* __restrict__ F2, int X, int Y, int Z, int Xp, int XYp,
+                                                const Cell32& cl, float out[3]) {
+    const int b = cl.base;
+    const bool ox = cl.gx + 1 < X, oy = cl.gy + 1 < Y, oz = cl.gz + 1 < Z;
+    const float* const F[3] = {F0, F1, F2};
+    float f[3][8];
+    if (ox && oy && oz) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            f[k][0] = __ldg(F[k] + b + 1 + Xp + XYp);
+            f[k][1] = __ldg(F[k] + b + 1 + Xp);
+            f[k][2] = __ldg(F[k] + b + 1 + XYp);
+            f[k][3] = __ldg(F[k] + b + 1);
+            f[k][4] = __ldg(F[k] + b + Xp + XYp);
+            f[k][5] = __ldg(F[k] + b + Xp);
+            f[k][6] = __ldg(F[k] + b + XYp);
+            f[k][7] = __ldg(F[k] + b);
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const float f0 = __ldg(F[k]);
+            f[k][0] = (ox && oy && oz) ? __ldg(F[k] + b + 1 + Xp + XYp) : f0;
+            f[k][1] = (ox && oy) ? __ldg(F[k] + b + 1 + Xp) : f0;
+            f[k][2] = (ox && oz) ? __ldg(F[k] + b + 1 + XYp) : f0;
+            f[k][3] = ox ? __ldg(F[k] + b + 1) : f0;
+            f[k][4] = (oy && oz) ? __ldg(F[k] + b + Xp + XYp) : f0;
+            f[k][5] = oy ? __ldg(F[k] + b + Xp) : f0;
+            f[k][6] = oz ? __ldg(F[k] + b + XYp) : f0;
+            f[k][7] = __ldg(F[k] + b);
+        }
+    }
+    trilerp3(f, cl.a, cl.b, cl.c, out);
 }
 
 // tri_checked with 32-bit indices: corners outside the grid read element 0.  X, Y, Z:
@@ -194,8 +264,14 @@ __device__ __forceinline__ float4 tri_unchecked32_f4(const float4* __restrict__ 
     }
     const float4 f111 = __ldg(F + o111), f110 = __ldg(F + o110), f101 = __ldg(F + o101), f100 = __ldg(F + o100);
     const float4 f011 = __ldg(F + o011), f010 = __ldg(F + o010), f001 = __ldg(F + o001), f000 = __ldg(F + b);
-    return lerp4_(lerp4_(lerp4_(f111, f110, cl.c), lerp4_(f101, f100, cl.c), cl.b),
-                  lerp4_(lerp4_(f011, f010, cl.c), lerp4_(f001, f000, cl.c), cl.b), cl.a);
+    // channels (x, y) and (z, w) as packed pairs: per channel the lerp4_ arithmetic
+    auto lo = [](float4 v) { return make_float2(v.x, v.y); };
+    auto hi = [](float4 v) { return make_float2(v.z, v.w); };
+    const float2 r0 = trilerp2(lo(f111), lo(f110), lo(f101), lo(f100), lo(f011), lo(f010), lo(f001), lo(f000), cl.a,
+                               cl.b, cl.c);
+    const float2 r1 = trilerp2(hi(f111), hi(f110), hi(f101), hi(f100), hi(f011), hi(f010), hi(f001), hi(f000), cl.a,
+                               cl.b, cl.c);
+    return make_float4(r0.x, r0.y, r1.x, r1.y);
 }
 
 // Hint that the 128-byte line holding *p will be read soon: it is fetched into L2 with

@@ -281,11 +281,17 @@ __global__ void __launch_bounds__(256) warp4_kernel(const float* __restrict__ po
             for (int j = 0; j < 8; ++j) f[k][j] = __ldg(img + o[j]);
             if (out_lab) lb[k] = __ldg(lab + b);
         }
+        // voxels (0, 1) and (2, 3) as packed pairs, each lane with its own cell: per voxel
+        // exactly trilerp
         float r[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k)
-            r[k] = trilerp(f[k][0], f[k][1], f[k][2], f[k][3], f[k][4], f[k][5], f[k][6], f[k][7], cl[k].a, cl[k].b,
-                           cl[k].c);
+        for (int k = 0; k < 4; k += 2) {
+            auto p = [&](int q) { return make_float2(f[k][q], f[k + 1][q]); };
+            const float2 v = trilerp2w(p(0), p(1), p(2), p(3), p(4), p(5), p(6), p(7), make_float2(cl[k].a, cl[k + 1].a),
+                                       make_float2(cl[k].b, cl[k + 1].b), make_float2(cl[k].c, cl[k + 1].c));
+            r[k] = v.x;
+            r[k + 1] = v.y;
+        }
         __stcs(reinterpret_cast<float4*>(out) + t, make_float4(r[0], r[1], r[2], r[3]));  // written once
         if (out_lab) {
             short4 l;

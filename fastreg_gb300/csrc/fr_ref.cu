@@ -698,9 +698,11 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
 #pragma unroll
                         for (int c = 0; c < 3; ++c) prefetch_l2(Q[c] + i + 2 * XYp);
                 }
-                const float ux = a.alpha * tri_checked32(V[0], X, Y, Z, Xp, XYp, cl);
-                const float uy = a.alpha * tri_checked32(V[1], X, Y, Z, Xp, XYp, cl);
-                const float uz = a.alpha * tri_checked32(V[2], X, Y, Z, Xp, XYp, cl);
+                float vp[3];
+                tri_checked32_3(V[0], V[1], V[2], X, Y, Z, Xp, XYp, cl, vp);
+                const float ux = a.alpha * vp[0];
+                const float uy = a.alpha * vp[1];
+                const float uz = a.alpha * vp[2];
                 Q[0][i] = px + ux;
                 Q[1][i] = py + uy;
                 Q[2][i] = pz + uz;

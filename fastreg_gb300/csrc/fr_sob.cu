@@ -699,15 +699,22 @@ __global__ void __launch_bounds__(256) sob_pass_b_kernel(SobIterArgs a) {
                         for (int c = 0; c < 3; ++c) prefetch_l2(phi[c] + i + 2 * XY);
                 }
                 float u[3];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float* __restrict__ F = mc[c];
+                {  // components 0 and 1 interpolated as one packed pair (trilerp3)
                     const int b = (int)s.base;
-                    u[c] = lerpf_(lerpf_(lerpf_(__ldg(F + b + 1 + X + XY), __ldg(F + b + 1 + X), s.c),
-                                         lerpf_(__ldg(F + b + 1 + XY), __ldg(F + b + 1), s.c), s.b),
-                                  lerpf_(lerpf_(__ldg(F + b + X + XY), __ldg(F + b + X), s.c),
-                                         lerpf_(__ldg(F + b + XY), __ldg(F + b), s.c), s.b),
-                                  s.a);
+                    float f[3][8];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float* __restrict__ F = mc[c];
+                        f[c][0] = __ldg(F + b + 1 + X + XY);
+                        f[c][1] = __ldg(F + b + 1 + X);
+                        f[c][2] = __ldg(F + b + 1 + XY);
+                        f[c][3] = __ldg(F + b + 1);
+                        f[c][4] = __ldg(F + b + X + XY);
+                        f[c][5] = __ldg(F + b + X);
+                        f[c][6] = __ldg(F + b + XY);
+                        f[c][7] = __ldg(F + b);
+                    }
+                    trilerp3(f, s.a, s.b, s.c, u);
                 }
                 phi[0][i] = px + u[0];
                 phi[1][i] = py + u[1];
