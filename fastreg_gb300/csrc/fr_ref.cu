@@ -300,8 +300,6 @@ __device__ __forceinline__ void pass_a_voxel(const RefIterArgs& a, const Pair& P
     // the rows it adds (two slices above the floor corner) are fetched into L2 now
     prefetch_l2(LT + min(cl.base + 2 * XYp, N - 1));
     prefetch_l2(LT + min(cl.base + 2 * XYp + Xp, N - 1));
-    const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
-    const float Lq[3] = {lt.x, lt.y, lt.z};
 
     // Jacobian of psi_inv, row r = d(psi_inv_r)/d(x, y, z), and its determinant
     float M[3][3];
@@ -323,10 +321,6 @@ __device__ __forceinline__ void pass_a_voxel(const RefIterArgs& a, const Pair& P
     const float gs[3] = {(Q(1, 4)[1] - Q(1, 4)[-1]) * 0.5f,
                          (Q(1, 4)[RW] - Q(1, 4)[-RW]) * 0.5f,
                          (Q(2, 4)[0] - Q(0, 4)[0]) * 0.5f};
-    const float diff = Si - Tq;
-    float gU[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (P.w_reg * Lq[c])) * det;
 
     // velocity and its 6 neighbours (vb[2] is slice z)
     float vc[3], vxm[3], vxp[3], vym[3], vyp[3], vzm[3], vzp[3];
@@ -387,6 +381,15 @@ __device__ __forceinline__ void pass_a_voxel(const RefIterArgs& a, const Pair& P
             dv[c] = -1.f * ((xx + yy) + zz);
         }
     }
+
+    // the potential gradient, from the gathered (L, T) o psi_inv: used as late as the
+    // arithmetic allows, so that the work above overlaps the gather's latency
+    const float Tq = a.first_iter ? __ldg(Tg + i) : lt.w;
+    const float Lq[3] = {lt.x, lt.y, lt.z};
+    const float diff = Si - Tq;
+    float gU[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gU[c] = ((diff * gs[c]) + (P.w_reg * Lq[c])) * det;
 
     // velocity update (solver.cu:198-209) and psi_inv update (solver.cu:275-277)
     const float qd = a.m2 / (fabsf(rho_new) + 1e-5f);

@@ -137,17 +137,8 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                 const float f010 = __ldg(S + b + Xp), f110 = __ldg(S + b + 1 + Xp);
                 const float f001 = __ldg(S + b + XYp), f101 = __ldg(S + b + 1 + XYp);
                 const float f011 = __ldg(S + b + Xp + XYp), f111 = __ldg(S + b + 1 + Xp + XYp);
-                const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
-                const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
-                const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
-                const float W = lerpf_(A1, A0, s.a);
-                const float dWa = s.in_x ? A1 - A0 : 0.f;
-                const float dWb = s.in_y ? lerpf_(e11 - e10, e01 - e00, s.a) : 0.f;
-                const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
-                                                  lerpf_(f011 - f010, f001 - f000, s.b), s.a)
-                                         : 0.f;
-                const float r = W - tring[s0 * kGTPlane + ty * kTileX + tx];
                 // graph Laplacian of u = phi - x, neighbours inside the grid, order -x,+x,-y,+y,-z,+z
+                // (shared-memory work placed between the corner loads and their use)
                 const bool ok[6] = {x > 0, x < P.X - 1, y > 0, y < Y - 1, z > 0, z < Z - 1};
                 float lap[3];
 #pragma unroll
@@ -166,6 +157,16 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                     }
                     lap[c] = acc;
                 }
+                const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
+                const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
+                const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
+                const float W = lerpf_(A1, A0, s.a);
+                const float dWa = s.in_x ? A1 - A0 : 0.f;
+                const float dWb = s.in_y ? lerpf_(e11 - e10, e01 - e00, s.a) : 0.f;
+                const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
+                                                  lerpf_(f011 - f010, f001 - f000, s.b), s.a)
+                                         : 0.f;
+                const float r = W - tring[s0 * kGTPlane + ty * kTileX + tx];
                 G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
                 G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
                 G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
@@ -262,16 +263,6 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
                 const float f010 = __ldg(S + b + Xp), f110 = __ldg(S + b + 1 + Xp);
                 const float f001 = __ldg(S + b + XYp), f101 = __ldg(S + b + 1 + XYp);
                 const float f011 = __ldg(S + b + Xp + XYp), f111 = __ldg(S + b + 1 + Xp + XYp);
-                const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
-                const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
-                const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
-                const float W = lerpf_(A1, A0, s.a);
-                const float dWa = s.in_x ? A1 - A0 : 0.f;
-                const float dWb = s.in_y ? lerpf_(e11 - e10, e01 - e00, s.a) : 0.f;
-                const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
-                                                  lerpf_(f011 - f010, f001 - f000, s.b), s.a)
-                                         : 0.f;
-                const float r = W - q0[kGBTOff + ty * kTileX + tx];
                 const bool okn[6] = {x > 0, x < P.X - 1, y > 0, y < Y - 1, z > 0, z < Z - 1};
                 float lap[3];
 #pragma unroll
@@ -288,6 +279,16 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
                     }
                     lap[c] = acc;
                 }
+                const float e11 = lerpf_(f111, f110, s.c), e10 = lerpf_(f101, f100, s.c);
+                const float e01 = lerpf_(f011, f010, s.c), e00 = lerpf_(f001, f000, s.c);
+                const float A1 = lerpf_(e11, e10, s.b), A0 = lerpf_(e01, e00, s.b);
+                const float W = lerpf_(A1, A0, s.a);
+                const float dWa = s.in_x ? A1 - A0 : 0.f;
+                const float dWb = s.in_y ? lerpf_(e11 - e10, e01 - e00, s.a) : 0.f;
+                const float dWc = s.in_z ? lerpf_(lerpf_(f111 - f110, f101 - f100, s.b),
+                                                  lerpf_(f011 - f010, f001 - f000, s.b), s.a)
+                                         : 0.f;
+                const float r = W - q0[kGBTOff + ty * kTileX + tx];
                 G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
                 G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
                 G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
