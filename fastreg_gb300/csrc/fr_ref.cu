@@ -444,22 +444,24 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
         auto qslot = [](int zs) { return ((zs % kQS) + kQS) % kQS; };
         const int gv = stage_offset<kVH>(threadIdx.x, Y, Xp, x0, y0);
         const int gq = stage_offset<kQH>(threadIdx.x, Y, Xp, x0, y0);
-        auto stage_v = [&](int zs) {  // slice zs of v's three components
+        auto stage_v_at = [&](int zs, int sl) {  // slice zs of v's three components into slot sl
             if (gv < 0 || zs < 0 || zs >= Z) return;
-            float* dst = sm.v + vslot(zs) * kVPlane + 4 * threadIdx.x;
+            float* dst = sm.v + sl * kVPlane + 4 * threadIdx.x;
             const int off = gv + XYp * zs;
 #pragma unroll
             for (int c = 0; c < 3; ++c) cp_async16(dst + c * kVS * kVPlane, Vg[c] + off);
         };
-        auto stage_q = [&](int zs) {  // slice zs of psi_inv's three components, rho and S
+        auto stage_v = [&](int zs) { stage_v_at(zs, vslot(zs)); };
+        auto stage_q_at = [&](int zs, int sl) {  // slice zs of psi_inv's three components, rho and S
             if (gq < 0 || zs < 0 || zs >= Z) return;
-            float* dst = sm.q + qslot(zs) * kQPlane + 4 * threadIdx.x;
+            float* dst = sm.q + sl * kQPlane + 4 * threadIdx.x;
             const int off = gq + XYp * zs;
 #pragma unroll
             for (int c = 0; c < 3; ++c) cp_async16(dst + c * kQS * kQPlane, Qg[c] + off);
             cp_async16(dst + 3 * kQS * kQPlane, Rg + off);
             cp_async16(dst + 4 * kQS * kQPlane, Sg + off);
         };
+        auto stage_q = [&](int zs) { stage_q_at(zs, qslot(zs)); };
 
         __syncthreads();  // the previous tile is done with the ring buffers
         // prologue: everything slice zs0 needs, then what each of the next kAhead - 1
@@ -474,39 +476,40 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_kernel(RefIterArgs a) {
             cp_async_commit();
         }
 
-        // ring positions of slice z - 2 (v) and z - 1 (psi_inv), advanced per slice
-        int sv = vslot(zs0 - 2), sq = qslot(zs0 - 1);
+        // this thread's column in the staged slices z - 2 .. z + 2 of v and z - 1 .. z + 1 of
+        // psi_inv/rho/S, rotated by one slice per step; with one slice in flight, the slice
+        // staged at step z (z + 3 of v, z + 2 of psi_inv) goes into the slot of slice z - 3 /
+        // z - 2, and that slot is the newest one read at step z + 1
+        static_assert(kAhead == 1 && kVS == 6 && kQS == 4, "the slot rotation below assumes these rings");
         const int vc0 = (ty + kVH) * kVW + tx + kXO;
         const int qc0 = (ty + kQH) * kQW + tx + kXO;
+        const float* vb[5];
+        const float* qb[3];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) vb[k] = sm.v + vslot(zs0 - 2 + k) * kVPlane + vc0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) qb[k] = sm.q + qslot(zs0 - 1 + k) * kQPlane + qc0;
+        int sv = vslot(zs0 - 3), sq = qslot(zs0 - 2);  // the slots step zs0 stages into
         for (int z = zs0; z < zs1; ++z) {
             cp_async_wait<kAhead - 1>();  // slice z's group has landed (the newer ones may not)
             __syncthreads();              // ... for every thread, and slice z - 3 / z - 2 is no longer read
-            // prefetch what slice z + kAhead adds, into the slots of slices z - 3 (v) and z - 2
-            if (z + 2 + kAhead <= zs1 + 1) stage_v(z + 2 + kAhead);  // the last slice reads v up to zs1 + 1
-            if (z + 1 + kAhead <= zs1) stage_q(z + 1 + kAhead);      // and psi_inv up to zs1
+            // prefetch what slice z + 1 adds, into the slots of slices z - 3 (v) and z - 2
+            if (z + 3 <= zs1 + 1) stage_v_at(z + 3, sv);  // the last slice reads v up to zs1 + 1
+            if (z + 2 <= zs1) stage_q_at(z + 2, sq);      // and psi_inv up to zs1
             cp_async_commit();
             if (active) {
                 const int i = x + Xp * y + XYp * z;
-                // per-slice base pointers into the rings (immediate offsets from them)
-                const float* vb[5];
-#pragma unroll
-                for (int k = 0; k < 5; ++k) {
-                    int sl = sv + k;
-                    sl = sl >= kVS ? sl - kVS : sl;
-                    vb[k] = sm.v + sl * kVPlane + vc0;
-                }
-                const float* qb[3];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    int sl = sq + k;
-                    sl = sl >= kQS ? sl - kQS : sl;
-                    qb[k] = sm.q + sl * kQPlane + qc0;
-                }
                 pass_a_voxel<kVS * kVPlane, kQS * kQPlane, 3 * kQS * kQPlane, 4 * kQS * kQPlane, kVW>(
                     a, P, X, Y, Z, N, Xp, XYp, y, z, i, dv_xy, vb, qb, LT, Tg, Sg, Rg, Vg, rho_n, Vn, Qn);
             }
+#pragma unroll
+            for (int k = 0; k < 4; ++k) vb[k] = vb[k + 1];
+            vb[4] = sm.v + sv * kVPlane + vc0;
+            qb[0] = qb[1];
+            qb[1] = qb[2];
+            qb[2] = sm.q + sq * kQPlane + qc0;
             sv = sv + 1 == kVS ? 0 : sv + 1;
-            sq = sq + 1 == kQS ? 0 : sq + 1;
+            sq = (sq + 1) & 3;
         }
         cp_async_wait<0>();
     }
