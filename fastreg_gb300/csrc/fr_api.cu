@@ -93,6 +93,7 @@ struct fr_handle {
     unsigned int* dev_err = nullptr;  // device error word of the staged kernels
     bool tma_ok = false;            // the maps of this cohort are encoded (else only variant 0 runs)
     double* tile_partials = nullptr;
+    int* pair_tiles = nullptr;  // [npairs + 1] first I/O tile of each pair
     long long* tile_folds = nullptr;
     unsigned long long* dice = nullptr;
     double* pair_energy = nullptr;
@@ -499,6 +500,7 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     add((void**)&h->dev_err, sizeof(unsigned int));
     add((void**)&h->tmaps, sizeof(CUtensorMap) * (size_t)n * frg::TM_COUNT);
     add((void**)&h->tile_partials, sizeof(double) * 2 * ntiles);
+    add((void**)&h->pair_tiles, sizeof(int) * (n + 1));
     add((void**)&h->tile_folds, sizeof(long long) * ntiles);
     add((void**)&h->dice, sizeof(unsigned long long) * (size_t)n * (2 * 256 + 1));
     add((void**)&h->pair_energy, sizeof(double) * 2 * n);
@@ -525,6 +527,12 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     FR_CUDA(h, cudaMemset(h->block, 0, total));
     FR_CUDA(h, cudaMemcpy(h->d_pairs, h->hpairs.data(), sizeof(Pair) * n, cudaMemcpyHostToDevice));
     FR_CUDA(h, cudaMemcpy(h->d_tiles, h->htiles.data(), sizeof(Tile) * ntiles, cudaMemcpyHostToDevice));
+    {
+        std::vector<int> first(n + 1, ntiles);
+        for (int t = ntiles - 1; t >= 0; --t) first[h->htiles[t].x] = t;
+        for (int p = n - 1; p >= 0; --p) first[p] = std::min(first[p], first[p + 1]);
+        FR_CUDA(h, cudaMemcpy(h->pair_tiles, first.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    }
     if (h->P.solver == FR_SOLVER_REFERENCE) {
         FR_CUDA(h, cudaFuncSetAttribute((const void*)frg::ref_pass_a_kernel,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -705,6 +713,7 @@ frg::IoArgs io_args(fr_handle* h) {
     a.max_iter = h->last_iter;
     a.no_labels = h->P.no_labels;
     a.tile_partials = h->tile_partials;
+    a.pair_tiles = h->pair_tiles;
     a.tile_folds = h->tile_folds;
     a.dice = h->dice;
     a.pair_energy = h->pair_energy;

@@ -208,19 +208,24 @@ __global__ void __launch_bounds__(256) finalize_kernel(IoArgs a) {
     __syncthreads();
     if (!last) return;
     __threadfence();
-    // tiles are ordered by pair; one thread per pair sums its tiles in order
-    for (int p = tid; p < a.npairs; p += blockDim.x) {
-        double ed = 0.0, er = 0.0;
-        long long f = 0;
-        for (int t = 0; t < a.ntiles; ++t) {
-            if (a.tiles[t].x != p) continue;
+    // a pair's tiles are contiguous (the table is ordered by pair): the whole block sums
+    // them, each thread a fixed strided subset in order, then a fixed shuffle tree -- the
+    // same sums on every run
+    for (int p = 0; p < a.npairs; ++p) {
+        double ed = 0.0, er = 0.0, f = 0.0;  // fold counts stay exact in FP64 (< 2^53)
+        for (int t = a.pair_tiles[p] + tid; t < a.pair_tiles[p + 1]; t += blockDim.x) {
             ed += a.tile_partials[2 * (long long)t];
             er += a.tile_partials[2 * (long long)t + 1];
-            f += a.tile_folds[t];
+            f += (double)a.tile_folds[t];
         }
-        a.pair_energy[2 * p] = 0.5 * ed;
-        a.pair_energy[2 * p + 1] = 0.5 * er;
-        a.pair_folds[p] = f;
+        ed = block_sum_f64(ed, red);
+        er = block_sum_f64(er, red);
+        f = block_sum_f64(f, red);
+        if (tid == 0) {
+            a.pair_energy[2 * p] = 0.5 * ed;
+            a.pair_energy[2 * p + 1] = 0.5 * er;
+            a.pair_folds[p] = (long long)f;
+        }
     }
     if (tid == 0) *a.counter = 0u;
 }

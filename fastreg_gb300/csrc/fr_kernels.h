@@ -125,6 +125,7 @@ struct IoArgs {
     int no_labels;
     double* tile_partials;      // [ntiles][2]: e_data, e_reg
     long long* tile_folds;      // [ntiles]
+    const int* pair_tiles;      // [npairs + 1]: the first tile of each pair (tiles are ordered by pair)
     unsigned long long* dice;   // [npairs][2*256 + 1]: inter, count, out of range
     double* pair_energy;        // [npairs][2]
     long long* pair_folds;      // [npairs]
