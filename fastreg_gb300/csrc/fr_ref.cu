@@ -692,18 +692,6 @@ __global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
                     nz = Q[2][i + XYp];
                 }
                 const Cell32 cl = locate32(X, Y, Z, Xp, px, py, pz);
-                {  // L2 prefetch: the v rows the next slice's cell adds (psi is smooth, so that
-                   // cell is about this one plus a slice) and psi two slices on
-                    const int N = (int)P.N, o0 = min(cl.base + 2 * XYp, N - 1), o1 = min(cl.base + 2 * XYp + Xp, N - 1);
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        prefetch_l2(V[c] + o0);
-                        prefetch_l2(V[c] + o1);
-                    }
-                    if (z + 2 < Z)
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) prefetch_l2(Q[c] + i + 2 * XYp);
-                }
                 float vp[3];
                 tri_checked32_3(V[0], V[1], V[2], X, Y, Z, Xp, XYp, cl, vp);
                 const float ux = a.alpha * vp[0];
