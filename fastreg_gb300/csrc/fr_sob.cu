@@ -307,6 +307,52 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
     }
 }
 
+// The x pass of one staged slice: the K-tap filter along x of each of its 3 H staged rows
+// (WS columns; column s holds x = x0 - HX + s) into 32 outputs per row of Gx.  Task (row rr,
+// group gq) computes outputs 4 gq .. 4 gq + 3 of row rr from 1 + HX / 2 aligned 16-byte
+// shared-memory loads (one load per tap and output before).  On a tile at an x edge the
+// columns outside [0, X) read the edge column (the replicate boundary).  row_of(rr): the
+// staged row that Gx row rr filters.  Each output is the chain acc = fma(w_q, g_q, acc),
+// q = 0 .. K - 1.
+template <int R, typename RowOf>
+__device__ __forceinline__ void smooth_x_pass(const SobIterArgs& a, RowOf row_of, float* __restrict__ dst,
+                                              bool xedge, int x0, int X) {
+    constexpr int HX = (R + 3) / 4 * 4, WS = kTileX + 2 * HX, H = kSobTileY + 2 * R, K = 2 * R + 1;
+    constexpr int NQ = 1 + HX / 2, NV = 4 * NQ;  // loads and values per task
+    static_assert(HX - R + 3 + K - 1 < NV, "a task's taps lie in its loads");
+    for (int task = threadIdx.x; task < 3 * H * (kTileX / 4); task += blockDim.x) {
+        const int rr = task / (kTileX / 4), gq = task % (kTileX / 4);
+        const float* row = row_of(rr);
+        float v[NV];
+#pragma unroll
+        for (int u = 0; u < NQ; ++u) {
+            const float4 f = *reinterpret_cast<const float4*>(row + 4 * gq + 4 * u);
+            v[4 * u] = f.x;
+            v[4 * u + 1] = f.y;
+            v[4 * u + 2] = f.z;
+            v[4 * u + 3] = f.w;
+        }
+        if (xedge) {
+            const float lo = row[min(max(HX - x0, 0), WS - 1)];         // x = 0
+            const float hi = row[min(max(X - 1 - x0 + HX, 0), WS - 1)];  // x = X - 1
+#pragma unroll
+            for (int t = 0; t < NV; ++t) {
+                const int xt = x0 - HX + 4 * gq + t;
+                v[t] = xt < 0 ? lo : (xt > X - 1 ? hi : v[t]);
+            }
+        }
+        float out[4];
+#pragma unroll
+        for (int o = 0; o < 4; ++o) {
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], v[o + HX - R + q], acc);
+            out[o] = acc;
+        }
+        *reinterpret_cast<float4*>(dst + rr * kTileX + 4 * gq) = make_float4(out[0], out[1], out[2], out[3]);
+    }
+}
+
 // Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
 // fused with the momentum update m = damping * m - step * gs.  A block owns a 32 x 8
 // column tile and marches z.  Each input slice (the tile's rows plus an R halo, clamped
@@ -326,9 +372,8 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
     constexpr int NB = 4 * (3 * 3 * H * WS + 2 * 3 * H * kTileX) <= 48 * 1024 ? 3 : 2;  // staging buffers
     constexpr int NF = 3 * H * C;                      // chunks of one staged slice
     constexpr int NJ = (NF + 255) / 256;               // chunks per thread
-    constexpr int RW = (3 * H + kSobTileY - 1) / kSobTileY;  // x-pass rows per warp
     __shared__ __align__(16) float G[NB][3][H][WS];
-    __shared__ float Gx[2][3][H][kTileX];
+    __shared__ __align__(16) float Gx[2][3][H][kTileX];
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
 
     for (int t = blockIdx.x; t < a.ntiles_s; t += gridDim.x) {
@@ -367,47 +412,9 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
                 if (goff[j] >= 0) cp_async16(dst + 4 * f, g0 + (f / (H * C)) * NT + zoff + goff[j]);
             }
         };
-        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
+        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
             const float* src = &G[k % NB][0][0][0];
-            float* dst = &Gx[k & 1][0][0][0];
-            // rows ty + 8 j, two at a time as one packed pair (per lane the same fused
-            // multiply-adds as one row at a time)
-#pragma unroll
-            for (int j = 0; j < RW; j += 2) {
-                const int r0 = ty + kSobTileY * j, r1 = r0 + kSobTileY;  // rows of the 3 H staged rows
-                if (j + 1 < RW && r1 < 3 * H) {
-                    const float *w0 = src + r0 * WS, *w1 = src + r1 * WS;
-                    float2 acc = make_float2(0.f, 0.f);
-                    if (!xedge) {
-#pragma unroll
-                        for (int q = 0; q < K; ++q)
-                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]),
-                                             make_float2(w0[HX - R + tx + q], w1[HX - R + tx + q]), acc);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) {
-                            const int xi = min(max(x0 - R + tx + q, 0), X - 1) - (x0 - HX);
-                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]), make_float2(w0[xi], w1[xi]), acc);
-                        }
-                    }
-                    dst[r0 * kTileX + tx] = acc.x;
-                    dst[r1 * kTileX + tx] = acc.y;
-                } else if (r0 < 3 * H) {
-                    const float* row = src + r0 * WS;
-                    float acc = 0.f;
-                    if (!xedge) {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], row[HX - R + tx + q], acc);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) {
-                            const int xi = min(max(x0 - R + tx + q, 0), X - 1);
-                            acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
-                        }
-                    }
-                    dst[r0 * kTileX + tx] = acc;
-                }
-            }
+            smooth_x_pass<R>(a, [&](int rr) { return src + rr * WS; }, &Gx[k & 1][0][0][0], xedge, x0, X);
         };
 
         // this thread's column; its momentum is loaded one output slice ahead
@@ -500,9 +507,8 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
     constexpr int NT = 4 * (4 * BSTRIDE + 2 * 3 * H * kTileX) + 32 <= 48 * 1024   ? 4
                        : 4 * (3 * BSTRIDE + 2 * 3 * H * kTileX) + 24 <= 48 * 1024 ? 3
                                                                                   : 2;
-    constexpr int RW = (3 * H + kSobTileY - 1) / kSobTileY;
     __shared__ __align__(128) float G[NT][BSTRIDE];
-    __shared__ float Gx[2][3][H][kTileX];
+    __shared__ __align__(16) float Gx[2][3][H][kTileX];
     __shared__ __align__(8) uint64_t full[NT];
     typedef SliceRing<NT> Ring;
     const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
@@ -532,52 +538,15 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
             tma_load_4d(&G[Ring::slot(n)][0], mg, x0 - HX, y0 - R, min(max(zt0 - R + k, 0), Z - 1), 0, bar);
             ++issued;
         };
-        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1], RW rows per warp
+        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
             const float* src = &G[Ring::slot(nbase + (unsigned)k)][0];
-            float* dst = &Gx[k & 1][0][0][0];
-            // staged row rr holds the clamped row of component c: rows two at a time as one
-            // packed pair, as in sob_smooth3_kernel
+            // staged row rr holds row r of component c, but the filter reads the clamped row
             auto row_of = [&](int rr) {
                 const int c = rr / H, r = rr - c * H;
-                const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);  // the clamped row
+                const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);
                 return src + (c * H + rs) * WS;
             };
-#pragma unroll
-            for (int j = 0; j < RW; j += 2) {
-                const int r0 = ty + kSobTileY * j, r1 = r0 + kSobTileY;
-                if (j + 1 < RW && r1 < 3 * H) {
-                    const float *w0 = row_of(r0), *w1 = row_of(r1);
-                    float2 acc = make_float2(0.f, 0.f);
-                    if (!xedge) {
-#pragma unroll
-                        for (int q = 0; q < K; ++q)
-                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]),
-                                             make_float2(w0[HX - R + tx + q], w1[HX - R + tx + q]), acc);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) {
-                            const int xi = min(max(x0 - R + tx + q, 0), X - 1) - (x0 - HX);
-                            acc = __ffma2_rn(make_float2(a.taps[q], a.taps[q]), make_float2(w0[xi], w1[xi]), acc);
-                        }
-                    }
-                    dst[r0 * kTileX + tx] = acc.x;
-                    dst[r1 * kTileX + tx] = acc.y;
-                } else if (r0 < 3 * H) {
-                    const float* row = row_of(r0);
-                    float acc = 0.f;
-                    if (!xedge) {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], row[HX - R + tx + q], acc);
-                    } else {
-#pragma unroll
-                        for (int q = 0; q < K; ++q) {
-                            const int xi = min(max(x0 - R + tx + q, 0), X - 1);
-                            acc = fmaf(a.taps[q], row[xi - (x0 - HX)], acc);
-                        }
-                    }
-                    dst[r0 * kTileX + tx] = acc;
-                }
-            }
+            smooth_x_pass<R>(a, row_of, &Gx[k & 1][0][0][0], xedge, x0, X);
         };
         auto wait = [&](int k) {
             return mbar_wait_bounded(full + Ring::slot(nbase + (unsigned)k), Ring::parity(nbase + (unsigned)k));
