@@ -1522,14 +1522,14 @@ int fr_warp(const float* d_pos, const float* d_img, const int16_t* d_lab, const 
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     auto aligned = [](const void* p, uintptr_t a) { return ((uintptr_t)p & (a - 1)) == 0; };
-    const bool vec4 = P.N % 4 == 0 && frg::fits_index32(P.X, P.Y, P.Z) && aligned(d_pos, 16) && aligned(d_out, 16) &&
-                      (!d_out_lab || aligned(d_out_lab, 8));
-    const void* fn = vec4 ? (const void*)frg::warp4_kernel : (const void*)frg::warp_kernel;
+    const bool vec2 = P.N % 2 == 0 && frg::fits_index32(P.X, P.Y, P.Z) && aligned(d_pos, 8) && aligned(d_out, 8) &&
+                      (!d_out_lab || aligned(d_out_lab, 4));
+    const void* fn = vec2 ? (const void*)frg::warp2_kernel : (const void*)frg::warp_kernel;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 256, 0);
-    const long long want = ((vec4 ? P.N / 4 : P.N) + 255) / 256;
+    const long long want = ((vec2 ? P.N / 2 : P.N) + 255) / 256;
     int grid = (int)std::max(1LL, std::min<long long>(want, (long long)std::max(per_sm, 1) * std::max(sms, 1)));
-    if (vec4)
-        frg::warp4_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_pos, d_img, d_lab, d_out, d_out_lab, P.X, P.Y, P.Z);
+    if (vec2)
+        frg::warp2_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_pos, d_img, d_lab, d_out, d_out_lab, P.X, P.Y, P.Z);
     else
         frg::warp_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_pos, d_img, d_lab, d_out, d_out_lab, P);
     cudaError_t e = cudaGetLastError();

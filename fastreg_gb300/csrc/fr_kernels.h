@@ -139,7 +139,7 @@ __global__ void finalize_kernel(IoArgs a);
 __global__ void warp_kernel(const float* __restrict__ pos, const float* __restrict__ img,
                             const int16_t* __restrict__ lab, float* __restrict__ out,
                             int16_t* __restrict__ out_lab, Pair P);
-__global__ void warp4_kernel(const float* pos, const float* img, const int16_t* lab, float* out, int16_t* out_lab, int X,
+__global__ void warp2_kernel(const float* pos, const float* img, const int16_t* lab, float* out, int16_t* out_lab, int X,
                              int Y, int Z);
 // the reference's unused field kernels (fr_fields.cu)
 __global__ void estimate_inverse_kernel(const float* psi, float* psi_inv, int X, int Y, int Z, int sweeps);

@@ -1,6 +1,6 @@
 // fr_limits.h -- when a volume may be addressed with 32-bit voxel indices.
 //
-// The 32-bit kernels (the solver kernels inside one pair, warp4_kernel) form corner and
+// The 32-bit kernels (the solver kernels inside one pair, warp2_kernel) form corner and
 // prefetch offsets from a cell's floor corner b <= N - 1 by adding up to two slices, a
 // row and one voxel (b + 1 + X + XY for the far corner of a cell, b + 2 XY + X for the
 // rows the next slice's cell adds), and only then clamp them to the last voxel.  Those
