@@ -914,6 +914,17 @@ int autotune(fr_handle* h, cudaStream_t s) {
         return fail(h, FR_ERR_CUDA, "autotune: cudaEventCreate failed");
     }
     Shapes best = default_shapes(h);
+    // tile depths: a fixed ladder, plus ceil(Zmax / k), which cut the tallest pair's columns
+    // into k tiles of (nearly) equal depth, so that the tile count can match the GPU's
+    // resident blocks more closely than the ladder's steps allow
+    std::vector<int> depths = {1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96};
+    {
+        int zmax = 1;
+        for (const Pair& P : h->hpairs) zmax = std::max(zmax, P.Z);
+        for (int k = 1; k <= 32; ++k) depths.push_back((zmax + k - 1) / k);
+        std::sort(depths.begin(), depths.end());
+        depths.erase(std::unique(depths.begin(), depths.end()), depths.end());
+    }
     int rc = FR_OK;
     for (int r : active_roles(h)) {
         std::vector<Shape> cand;
@@ -923,7 +934,7 @@ int autotune(fr_handle* h, cudaStream_t s) {
             if (occ > 1) bps.push_back(occ - 1);
             if (occ / 2 >= 1 && occ / 2 < occ - 1) bps.push_back(occ / 2);
             bps.push_back(-1);  // one block per tile
-            for (int depth : {1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96})
+            for (int depth : depths)
                 for (int b : bps) cand.push_back(Shape{depth, b, v});
         }
         // two passes over the candidates, each candidate's faster time kept (less noise)

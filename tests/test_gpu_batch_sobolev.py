@@ -99,6 +99,9 @@ def test_autotuned_shapes_do_not_change_results(cuda, solver):
     the fields are bit-identical to AUTOTUNE=0's default shapes, and the chosen shapes
     are among the candidates."""
     dims_list = [(41, 23, 29), (20, 18, 16)]
+    # the depth candidates: a fixed ladder and ceil(Zmax / k), k = 1..32 (Zmax = 29 here)
+    zmax = max(d[2] for d in dims_list)
+    candidates = {1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96} | {-(-zmax // k) for k in range(1, 33)}
     kw = dict(no_labels=4, max_iter=12, alpha=0.02, solver=solver, step=0.5, damping=0.9)
     pairs_np = [images(d, 700 + k) for k, d in enumerate(dims_list)]
     fields = []
@@ -108,7 +111,7 @@ def test_autotuned_shapes_do_not_change_results(cuda, solver):
         fr.register_batch(bufs)
         fields.append([fr.get_field(N.FR_FIELD_PSI, pair=k).cpu().numpy() for k in range(len(dims_list))])
         shapes = fr.tile_shapes()
-        assert all(d in (1, 2, 4, 8, 12, 16, 24, 32, 48, 64, 96) and (b >= 1 or b == -1) for d, b in shapes), shapes
+        assert all(d in candidates and (b >= 1 or b == -1) for d, b in shapes), shapes
         if not tune:
             default = (16, 24, 24) if solver == "reference" else (12, 32, 8)
             assert tuple(d for d, _ in shapes) == default, shapes
