@@ -201,8 +201,14 @@ __global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
         mbar_fence_init();
     }
     __syncthreads();
-    unsigned nbase = 0;    // slices this block has staged before the current tile
-    unsigned issued = 0;   // slices issued so far (thread 0's count)
+    // The block's slices go through the ring in one sequence n = 0, 1, 2, ... across its
+    // tiles (slot n % kTLS, the (n / kTLS)-th fill of that slot), issued by thread 0 and
+    // waited for by every thread in the same order; both walk it with counters instead of
+    // dividing: the next slot to issue (islot), the next slot to wait for (wslot), and per
+    // slot the parity of its next completion (bit k of wph).
+    unsigned issued = 0;  // slices issued so far (thread 0's count)
+    int islot = 0, wslot = 0;
+    unsigned wph = 0u;
     bool failed = false;
     for (int t = blockIdx.x; t < a.ntiles_l && !failed; t += gridDim.x) {
         const Tile tl = a.tiles_l[t];
@@ -216,15 +222,21 @@ __global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
         float4* LT = a.LT + P.off;
         const int x = tl.y + tx, y = tl.z + ty;
         const bool active = x >= 1 && x <= X - 2 && y >= 1 && y <= Y - 2;
-        const int nsl = zs1 - zs0 + 2;  // slices zs0 - 1 .. zs1
+        const int nsl = zs1 - zs0 + 2;  // slices zs0 - 1 .. zs1, all issued and all waited for
         auto issue = [&](int j) {       // slice zs0 - 1 + j of the tile (thread 0)
-            const unsigned n = nbase + (unsigned)j;
-            float* dst = ring + Ring::slot(n) * kTSlot;
-            uint64_t* bar = full + Ring::slot(n);
+            float* dst = ring + islot * kTSlot;
+            uint64_t* bar = full + islot;
             mbar_arrive_expect_tx(bar, kTLBytes);
             tma_load_4d(dst, mpsi, tl.y - 4, tl.z - 1, zs0 - 1 + j, 0, bar);
             tma_load_3d(dst + kTTOff, mT, tl.y, tl.z, zs0 - 1 + j, bar);
+            islot = islot + 1 == kTLS ? 0 : islot + 1;
             ++issued;
+        };
+        auto wait_next = [&]() {  // the next slice of the sequence has landed
+            const bool ok = mbar_wait_bounded(full + wslot, (wph >> wslot) & 1u);
+            wph ^= 1u << wslot;
+            wslot = wslot + 1 == kTLS ? 0 : wslot + 1;
+            return ok;
         };
         __syncthreads();  // the previous tile is done with the ring
         if (tid == 0) {
@@ -233,11 +245,23 @@ __global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
             for (int j = 0; j < min(nsl, kTLS); ++j) issue(j);
         }
         const int c0 = (ty + 1) * kTQW + tx + 4;
+        int sm = 0, s0 = 0, sp = 0;  // slots of slices j0, j0 + 1 and j0 + 2 of the tile
         for (int j0 = 0; j0 + 2 < nsl; ++j0) {
             // slices j0, j0 + 1 and j0 + 2 of the tile are read; j0 + 2 is the newest
-            bool ok = true;
-            for (int j = (j0 == 0 ? 0 : j0 + 2); j <= j0 + 2; ++j)
-                ok = ok && mbar_wait_bounded(full + Ring::slot(nbase + j), Ring::parity(nbase + j));
+            bool ok;
+            if (j0 == 0) {
+                sm = wslot;
+                ok = wait_next();
+                s0 = wslot;
+                ok = wait_next() && ok;
+                sp = wslot;
+                ok = wait_next() && ok;
+            } else {
+                sm = s0;
+                s0 = sp;
+                sp = wslot;
+                ok = wait_next();
+            }
             // every thread is past step j0 - 1 (the slot of slice j0 - 1 is free), and the
             // block agrees on whether any wait gave up
             if (__syncthreads_or(!ok)) {
@@ -247,9 +271,9 @@ __global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
             if (tid == 0 && j0 >= 1 && j0 - 1 + kTLS < nsl) issue(j0 - 1 + kTLS);
             if (active) {
                 const int z = zs0 + j0;
-                const float* qm = ring + Ring::slot(nbase + j0) * kTSlot + c0;
-                const float* q0 = ring + Ring::slot(nbase + j0 + 1) * kTSlot;
-                const float* qp = ring + Ring::slot(nbase + j0 + 2) * kTSlot + c0;
+                const float* qm = ring + sm * kTSlot + c0;
+                const float* q0 = ring + s0 * kTSlot;
+                const float* qp = ring + sp * kTSlot + c0;
                 float l[3];
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
@@ -267,7 +291,6 @@ __global__ void __launch_bounds__(256) ref_laplacian_tma_kernel(RefIterArgs a) {
                 LT[x + Xp * y + XYp * z] = make_float4(l[0], l[1], l[2], tv);
             }
         }
-        nbase += (unsigned)nsl;
     }
     if (failed && tid == 0) {
         // the copies this block issued and nobody waited for: wait for them (bounded)
