@@ -310,48 +310,70 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
 // The x pass of one staged slice: the K-tap filter along x of each of its 3 H staged rows
 // (WS columns; column s holds x = x0 - HX + s) into 32 outputs per row of Gx.  Task (row rr,
 // group gq) computes outputs 4 gq .. 4 gq + 3 of row rr from 1 + HX / 2 aligned 16-byte
-// shared-memory loads (one load per tap and output before).  On a tile at an x edge the
-// columns outside [0, X) read the edge column (the replicate boundary).  row_of(rr): the
-// staged row that Gx row rr filters.  Each output is the chain acc = fma(w_q, g_q, acc),
-// q = 0 .. K - 1.
-template <int R, typename RowOf>
-__device__ __forceinline__ void smooth_x_pass(const SobIterArgs& a, RowOf row_of, float* __restrict__ dst,
-                                              bool xedge, int x0, int X) {
-    constexpr int HX = (R + 3) / 4 * 4, WS = kTileX + 2 * HX, H = kSobTileY + 2 * R, K = 2 * R + 1;
-    constexpr int NQ = 1 + HX / 2, NV = 4 * NQ;  // loads and values per task
+// shared-memory loads (one load per tap and output before).  Thread e of the 256 takes
+// tasks e + 256 j, whose group is e & 7 and whose offsets in a staged slice and in Gx do not
+// change within a tile, so they are computed once per tile (init) rather than per slice.
+// On a tile at an x edge the columns outside [0, X) read the edge column (the replicate
+// boundary).  Each output is the chain acc = fma(w_q, g_q, acc), q = 0 .. K - 1.
+template <int R>
+struct SmoothXPass {
+    static constexpr int HX = (R + 3) / 4 * 4, WS = kTileX + 2 * HX, H = kSobTileY + 2 * R, K = 2 * R + 1;
+    static constexpr int NQ = 1 + HX / 2, NV = 4 * NQ;  // loads and values per task
+    static constexpr int NTASK = 3 * H * (kTileX / 4), NJ = (NTASK + 255) / 256;
     static_assert(HX - R + 3 + K - 1 < NV, "a task's taps lie in its loads");
-    for (int task = threadIdx.x; task < 3 * H * (kTileX / 4); task += blockDim.x) {
-        const int rr = task / (kTileX / 4), gq = task % (kTileX / 4);
-        const float* row = row_of(rr);
-        float v[NV];
+    int src[NJ];  // offset of task j's first load in a staged slice (-1: no task j)
+    int dst[NJ];  // offset of its four outputs in Gx
+
+    // row_off(rr): offset in a staged slice of the row that Gx row rr filters
+    template <typename RowOff>
+    __device__ __forceinline__ void init(RowOff row_off) {
+        const int gq = threadIdx.x & 7;
 #pragma unroll
-        for (int u = 0; u < NQ; ++u) {
-            const float4 f = *reinterpret_cast<const float4*>(row + 4 * gq + 4 * u);
-            v[4 * u] = f.x;
-            v[4 * u + 1] = f.y;
-            v[4 * u + 2] = f.z;
-            v[4 * u + 3] = f.w;
+        for (int j = 0; j < NJ; ++j) {
+            const int task = threadIdx.x + 256 * j, rr = task >> 3;
+            src[j] = task < NTASK ? row_off(rr) + 4 * gq : -1;
+            dst[j] = rr * kTileX + 4 * gq;
         }
-        if (xedge) {
-            const float lo = row[min(max(HX - x0, 0), WS - 1)];         // x = 0
-            const float hi = row[min(max(X - 1 - x0 + HX, 0), WS - 1)];  // x = X - 1
-#pragma unroll
-            for (int t = 0; t < NV; ++t) {
-                const int xt = x0 - HX + 4 * gq + t;
-                v[t] = xt < 0 ? lo : (xt > X - 1 ? hi : v[t]);
-            }
-        }
-        float out[4];
-#pragma unroll
-        for (int o = 0; o < 4; ++o) {
-            float acc = 0.f;
-#pragma unroll
-            for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], v[o + HX - R + q], acc);
-            out[o] = acc;
-        }
-        *reinterpret_cast<float4*>(dst + rr * kTileX + 4 * gq) = make_float4(out[0], out[1], out[2], out[3]);
     }
-}
+
+    __device__ __forceinline__ void run(const SobIterArgs& a, const float* __restrict__ slice, float* __restrict__ gx,
+                                        bool xedge, int x0, int X) const {
+        const int gq = threadIdx.x & 7;
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+            if (src[j] < 0) continue;
+            const float* p = slice + src[j];
+            float v[NV];
+#pragma unroll
+            for (int u = 0; u < NQ; ++u) {
+                const float4 f = *reinterpret_cast<const float4*>(p + 4 * u);
+                v[4 * u] = f.x;
+                v[4 * u + 1] = f.y;
+                v[4 * u + 2] = f.z;
+                v[4 * u + 3] = f.w;
+            }
+            if (xedge) {
+                const float* row = p - 4 * gq;
+                const float lo = row[min(max(HX - x0, 0), WS - 1)];         // x = 0
+                const float hi = row[min(max(X - 1 - x0 + HX, 0), WS - 1)];  // x = X - 1
+#pragma unroll
+                for (int t = 0; t < NV; ++t) {
+                    const int xt = x0 - HX + 4 * gq + t;
+                    v[t] = xt < 0 ? lo : (xt > X - 1 ? hi : v[t]);
+                }
+            }
+            float out[4];
+#pragma unroll
+            for (int o = 0; o < 4; ++o) {
+                float acc = 0.f;
+#pragma unroll
+                for (int q = 0; q < K; ++q) acc = fmaf(a.taps[q], v[o + HX - R + q], acc);
+                out[o] = acc;
+            }
+            *reinterpret_cast<float4*>(gx + dst[j]) = make_float4(out[0], out[1], out[2], out[3]);
+        }
+    }
+};
 
 // Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
 // fused with the momentum update m = damping * m - step * gs.  A block owns a 32 x 8
@@ -364,8 +386,9 @@ __device__ __forceinline__ void smooth_x_pass(const SobIterArgs& a, RowOf row_of
 // of 2R + 1 slices that the z pass reads).  Columns outside [0, X) are read at the
 // clamped column (only tiles at the x edges take that path).  Each tap is one fused
 // multiply-add, acc = fma(w_k, g_k, acc), taken in the order k = -R..R for every axis.
+// Held to 5 resident blocks per SM (48 registers at R = 3), as is the TMA variant.
 template <int R>
-__global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
+__global__ void __launch_bounds__(256, 5) sob_smooth3_kernel(SobIterArgs a) {
     constexpr int HX = (R + 3) / 4 * 4;                // staged x halo: whole 16-byte chunks
     constexpr int WS = kTileX + 2 * HX, C = WS / 4;    // staged row: floats, chunks
     constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
@@ -412,9 +435,10 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
                 if (goff[j] >= 0) cp_async16(dst + 4 * f, g0 + (f / (H * C)) * NT + zoff + goff[j]);
             }
         };
+        SmoothXPass<R> xp;  // staged rows are already the clamped rows
+        xp.init([](int rr) { return rr * WS; });
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
-            const float* src = &G[k % NB][0][0][0];
-            smooth_x_pass<R>(a, [&](int rr) { return src + rr * WS; }, &Gx[k & 1][0][0][0], xedge, x0, X);
+            xp.run(a, &G[k % NB][0][0][0], &Gx[k & 1][0][0][0], xedge, x0, X);
         };
 
         // this thread's column; its momentum is loaded one output slice ahead
@@ -427,6 +451,14 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
 
         float2 ring01[K];  // the z ring of the y-pass results: components 0 and 1 packed, 2
         float ring2[K];
+        // zeroed: the shift below copies every slot from the first step on, before the slots
+        // near the end are filled, and a copy of an indeterminate value is undefined behaviour
+        // (a build at 48 registers turned it into wrong results)
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            ring01[q] = make_float2(0.f, 0.f);
+            ring2[q] = 0.f;
+        }
         __syncthreads();  // the previous tile is done with G and Gx
 #pragma unroll
         for (int k = 0; k < NB; ++k) {
@@ -497,7 +529,7 @@ __global__ void __launch_bounds__(256) sob_smooth3_kernel(SobIterArgs a) {
 // zeros that the copy writes outside the volume are never read.  Waits are bounded as in
 // ref_laplacian_tma_kernel.
 template <int R>
-__global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
+__global__ void __launch_bounds__(256, 5) sob_smooth3_tma_kernel(SobIterArgs a) {
     constexpr int HX = (R + 3) / 4 * 4;
     constexpr int WS = kTileX + 2 * HX;
     constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
@@ -538,15 +570,14 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
             tma_load_4d(&G[Ring::slot(n)][0], mg, x0 - HX, y0 - R, min(max(zt0 - R + k, 0), Z - 1), 0, bar);
             ++issued;
         };
+        SmoothXPass<R> xp;  // staged row rr holds row r of component c; the filter reads the clamped row
+        xp.init([&](int rr) {
+            const int c = rr / H, r = rr - c * H;
+            const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);
+            return (c * H + rs) * WS;
+        });
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
-            const float* src = &G[Ring::slot(nbase + (unsigned)k)][0];
-            // staged row rr holds row r of component c, but the filter reads the clamped row
-            auto row_of = [&](int rr) {
-                const int c = rr / H, r = rr - c * H;
-                const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);
-                return src + (c * H + rs) * WS;
-            };
-            smooth_x_pass<R>(a, row_of, &Gx[k & 1][0][0][0], xedge, x0, X);
+            xp.run(a, &G[Ring::slot(nbase + (unsigned)k)][0], &Gx[k & 1][0][0][0], xedge, x0, X);
         };
         auto wait = [&](int k) {
             return mbar_wait_bounded(full + Ring::slot(nbase + (unsigned)k), Ring::parity(nbase + (unsigned)k));
@@ -561,6 +592,14 @@ __global__ void __launch_bounds__(256) sob_smooth3_tma_kernel(SobIterArgs a) {
 
         float2 ring01[K];  // the z ring of the y-pass results: components 0 and 1 packed, 2
         float ring2[K];
+        // zeroed: the shift below copies every slot from the first step on, before the slots
+        // near the end are filled, and a copy of an indeterminate value is undefined behaviour
+        // (a build at 48 registers turned it into wrong results)
+#pragma unroll
+        for (int q = 0; q < K; ++q) {
+            ring01[q] = make_float2(0.f, 0.f);
+            ring2[q] = 0.f;
+        }
         __syncthreads();  // the previous tile is done with G and Gx
         if (tid == 0) {
             tma_prefetch_map(mg);
