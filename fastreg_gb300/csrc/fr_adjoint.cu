@@ -214,7 +214,7 @@ __global__ void adj_loss_kernel(AdjDims D, const float* __restrict__ S, const fl
         TriEval t;
         tri_eval(D, S, __ldg(phi + i), __ldg(phi + D.N + i), __ldg(phi + 2 * D.N + i), t, false);
         const float r = t.val - __ldg(T + i);
-        e += 0.5 * (double)r * (double)r;
+        e = fma(0.5 * (double)r, (double)r, e);  // (r / 2) * r is exact in FP64: same bits
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             const float mc = __ldg(m + (long long)c * D.N + i);

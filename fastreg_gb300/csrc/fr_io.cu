@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(IoArgs a) {
 
                 // data energy
                 const float df = __ldg(T + i) - ws;
-                ed += (double)df * (double)df;
+                ed = fma((double)df, (double)df, ed);  // df * df is exact in FP64: same bits
 
                 // deformation Jacobian with the mirrored one-sided boundary
                 int x1 = x + 1, x2 = x - 1, y1 = y + 1, y2 = y - 1, z1_ = z + 1, z2_ = z - 1;

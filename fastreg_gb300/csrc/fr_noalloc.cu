@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(256) stats_noalloc_kernel(const float* __restr
     for (long long i = blockIdx.x * (long long)blockDim.x + tid; i < N; i += (long long)gridDim.x * blockDim.x) {
         const int z = (int)(i / XY), y = (int)((i - z * XY) / X), x = (int)(i - z * XY - (long long)y * X);
         const float df = __ldg(T + i) - __ldg(wS + i);
-        ed += (double)df * (double)df;
+        ed = fma((double)df, (double)df, ed);  // df * df is exact in FP64: same bits
         // deformation Jacobian with the mirrored one-sided boundary (vector_fields.cu:537-585)
         int x1 = x + 1, x2 = x - 1, y1 = y + 1, y2 = y - 1, z1 = z + 1, z2 = z - 1;
         if (x == 0) x2 = x + 1; else if (x == X - 1) x1 = x - 1;

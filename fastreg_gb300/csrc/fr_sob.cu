@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(256) sob_grad_kernel(SobIterArgs a) {
                 G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
                 G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
                 G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
-                e += (double)r * (double)r;
+                e = fma((double)r, (double)r, e);  // r * r is exact in FP64: one DFMA, same bits
             }
             sm = s0;
         }
@@ -292,7 +292,7 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
                 G[0][i] = (r * dWa) + (P.w_reg * lap[0]);
                 G[1][i] = (r * dWb) + (P.w_reg * lap[1]);
                 G[2][i] = (r * dWc) + (P.w_reg * lap[2]);
-                e += (double)r * (double)r;
+                e = fma((double)r, (double)r, e);  // r * r is exact in FP64: one DFMA, same bits
             }
         }
         nbase += (unsigned)nsl;
