@@ -336,6 +336,8 @@ struct SmoothXPass {
         }
     }
 
+    // xedge: the tile touches an x edge and the staged columns outside [0, X) still hold
+    // whatever the staging left there (false when they already hold the edge values)
     __device__ __forceinline__ void run(const SobIterArgs& a, const float* __restrict__ slice, float* __restrict__ gx,
                                         bool xedge, int x0, int X) const {
         const int gq = threadIdx.x & 7;
@@ -373,6 +375,38 @@ struct SmoothXPass {
             *reinterpret_cast<float4*>(gx + dst[j]) = make_float4(out[0], out[1], out[2], out[3]);
         }
     }
+
+    // The replicate boundary written into a staged slice of a tile at an x edge.  Outputs
+    // outside [0, X) are never stored, so only the R staged columns beyond each edge that
+    // outputs inside it read need the edge value: x = -R .. -1 take x = 0's, x = X .. X - 1 + R
+    // take x = X - 1's.  One (row, side, column) item per thread, 3 H * 2 R items (252 at
+    // R = 3); the other staged columns outside the volume keep whatever the copy left there
+    // and reach only outputs that are discarded.  The edge columns are only read, so the
+    // threads need no ordering among themselves; the block barrier that precedes the
+    // slice's x pass orders the writes before it.
+    __device__ __forceinline__ static void fix_edges(float* slice, int x0, int X) {
+        if constexpr (R > 0) {
+            constexpr int NW = 3 * H * 2 * R;
+            const bool left = x0 == 0;        // x0 is a multiple of 32 and HX <= 8
+            const int shi = X - 1 - x0 + HX;  // column of x = X - 1
+#pragma unroll
+            for (int w0 = 0; w0 < NW; w0 += 256) {
+                const int w = w0 + (int)threadIdx.x;
+                if (w < NW) {
+                    const int rr = w / (2 * R), k = w - rr * (2 * R);
+                    float* row = slice + rr * WS;
+                    if (k < R) {
+                        if (left) row[HX - R + k] = row[HX];
+                    } else {
+                        const int c = shi + 1 + (k - R);
+                        if (c < WS) row[c] = row[shi];
+                    }
+                }
+            }
+            // these generic-proxy writes come before the tensor copy that next refills the slot
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+    }
 };
 
 // Separable Gaussian smoothing of g along x, y and z with the replicate boundary,
@@ -386,9 +420,14 @@ struct SmoothXPass {
 // of 2R + 1 slices that the z pass reads).  Columns outside [0, X) are read at the
 // clamped column (only tiles at the x edges take that path).  Each tap is one fused
 // multiply-add, acc = fma(w_k, g_k, acc), taken in the order k = -R..R for every axis.
-// Held to 5 resident blocks per SM (48 registers at R = 3), as is the TMA variant.
+// Resident blocks per SM the kernel is held to: as many as its (2R + 1)-slice ring and,
+// in this variant, the per-value edge selects of the x pass allow without spilling much
+// (5 blocks are 48 registers a thread, 4 are 64, 3 are 85).
 template <int R>
-__global__ void __launch_bounds__(256, 5) sob_smooth3_kernel(SobIterArgs a) {
+constexpr int kSmoothMinBlocksCp = R <= 3 ? 5 : (R <= 5 ? 4 : 3);
+
+template <int R>
+__global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel(SobIterArgs a) {
     constexpr int HX = (R + 3) / 4 * 4;                // staged x halo: whole 16-byte chunks
     constexpr int WS = kTileX + 2 * HX, C = WS / 4;    // staged row: floats, chunks
     constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
@@ -528,8 +567,13 @@ __global__ void __launch_bounds__(256, 5) sob_smooth3_kernel(SobIterArgs a) {
 // the row of the clamped y (inside the box whenever the tile is inside the volume); the
 // zeros that the copy writes outside the volume are never read.  Waits are bounded as in
 // ref_laplacian_tma_kernel.
+// The TMA variant writes the replicate boundary into the staged slice and runs the x pass
+// without selects: held to 5 resident blocks per SM up to R = 4 and 4 above.
 template <int R>
-__global__ void __launch_bounds__(256, 5) sob_smooth3_tma_kernel(SobIterArgs a) {
+constexpr int kSmoothMinBlocks = R <= 4 ? 5 : 4;
+
+template <int R>
+__global__ void __launch_bounds__(256, kSmoothMinBlocks<R>) sob_smooth3_tma_kernel(SobIterArgs a) {
     constexpr int HX = (R + 3) / 4 * 4;
     constexpr int WS = kTileX + 2 * HX;
     constexpr int H = kSobTileY + 2 * R, K = 2 * R + 1;
@@ -576,8 +620,11 @@ __global__ void __launch_bounds__(256, 5) sob_smooth3_tma_kernel(SobIterArgs a) 
             const int rs = min(max(y0 - R + r, 0), Y - 1) - (y0 - R);
             return (c * H + rs) * WS;
         });
-        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
-            xp.run(a, &G[Ring::slot(nbase + (unsigned)k)][0], &Gx[k & 1][0][0][0], xedge, x0, X);
+        auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1] (its edge columns already fixed)
+            xp.run(a, &G[Ring::slot(nbase + (unsigned)k)][0], &Gx[k & 1][0][0][0], false, x0, X);
+        };
+        auto fix_edges = [&](int k) {  // after slice k has landed, before the barrier that precedes its x pass
+            if (xedge) SmoothXPass<R>::fix_edges(&G[Ring::slot(nbase + (unsigned)k)][0], x0, X);
         };
         auto wait = [&](int k) {
             return mbar_wait_bounded(full + Ring::slot(nbase + (unsigned)k), Ring::parity(nbase + (unsigned)k));
@@ -605,15 +652,19 @@ __global__ void __launch_bounds__(256, 5) sob_smooth3_tma_kernel(SobIterArgs a) 
             tma_prefetch_map(mg);
             for (int k = 0; k < min(NT, nsl); ++k) issue(k);
         }
-        if (__syncthreads_or(!wait(0))) {  // slice 0 has landed
+        const bool ok0 = wait(0);  // slice 0 has landed
+        if (ok0) fix_edges(0);
+        if (__syncthreads_or(!ok0)) {
             failed = true;
             break;
         }
         x_pass(0);
         for (int k = 0; k < nsl; ++k) {
             const bool ok = k + 1 < nsl ? wait(k + 1) : true;  // slice k + 1 has landed
+            if (ok && k + 1 < nsl) fix_edges(k + 1);           // nobody reads its buffer before the barrier
             // every thread is past step k - 1: Gx[k & 1] is complete, slice k's buffer and
-            // Gx[(k + 1) & 1] are no longer read; and the block agrees on the waits
+            // Gx[(k + 1) & 1] are no longer read, slice k + 1's edge columns are written; and
+            // the block agrees on the waits
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
