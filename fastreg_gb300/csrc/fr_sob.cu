@@ -564,11 +564,11 @@ __global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel
 // thread NT - 1 slices ahead into a ring of NT buffers and completed on the buffer's
 // mbarrier.  Rows and slices outside the volume realise the replicate boundary: a slice
 // beyond an end is requested at the clamped z, and the x pass reads, for each staged row,
-// the row of the clamped y (inside the box whenever the tile is inside the volume); the
-// zeros that the copy writes outside the volume are never read.  Waits are bounded as in
-// ref_laplacian_tma_kernel.
-// The TMA variant writes the replicate boundary into the staged slice and runs the x pass
-// without selects: held to 5 resident blocks per SM up to R = 4 and 4 above.
+// the row of the clamped y (inside the box whenever the tile is inside the volume); along x,
+// the R columns beyond each edge are overwritten with the edge column in shared memory
+// once the slice has landed (SmoothXPass::fix_edges), so the x pass runs without selects.
+// Waits are bounded as in ref_laplacian_tma_kernel.  Held to 5 resident blocks per SM up
+// to R = 4 and 4 above.
 template <int R>
 constexpr int kSmoothMinBlocks = R <= 4 ? 5 : 4;
 
