@@ -313,8 +313,9 @@ __global__ void __launch_bounds__(256) sob_grad_tma_kernel(SobIterArgs a) {
 // shared-memory loads (one load per tap and output before).  Thread e of the 256 takes
 // tasks e + 256 j, whose group is e & 7 and whose offsets in a staged slice and in Gx do not
 // change within a tile, so they are computed once per tile (init) rather than per slice.
-// On a tile at an x edge the columns outside [0, X) read the edge column (the replicate
-// boundary).  Each output is the chain acc = fma(w_q, g_q, acc), q = 0 .. K - 1.
+// On a tile at an x edge the columns beyond the edges hold the edge column's value by the
+// time the x pass reads them (fix_edges: the replicate boundary).  Each output is the chain
+// acc = fma(w_q, g_q, acc), q = 0 .. K - 1.
 template <int R>
 struct SmoothXPass {
     static constexpr int HX = (R + 3) / 4 * 4, WS = kTileX + 2 * HX, H = kSobTileY + 2 * R, K = 2 * R + 1;
@@ -336,11 +337,8 @@ struct SmoothXPass {
         }
     }
 
-    // xedge: the tile touches an x edge and the staged columns outside [0, X) still hold
-    // whatever the staging left there (false when they already hold the edge values)
-    __device__ __forceinline__ void run(const SobIterArgs& a, const float* __restrict__ slice, float* __restrict__ gx,
-                                        bool xedge, int x0, int X) const {
-        const int gq = threadIdx.x & 7;
+    __device__ __forceinline__ void run(const SobIterArgs& a, const float* __restrict__ slice,
+                                        float* __restrict__ gx) const {
 #pragma unroll
         for (int j = 0; j < NJ; ++j) {
             if (src[j] < 0) continue;
@@ -353,16 +351,6 @@ struct SmoothXPass {
                 v[4 * u + 1] = f.y;
                 v[4 * u + 2] = f.z;
                 v[4 * u + 3] = f.w;
-            }
-            if (xedge) {
-                const float* row = p - 4 * gq;
-                const float lo = row[min(max(HX - x0, 0), WS - 1)];         // x = 0
-                const float hi = row[min(max(X - 1 - x0 + HX, 0), WS - 1)];  // x = X - 1
-#pragma unroll
-                for (int t = 0; t < NV; ++t) {
-                    const int xt = x0 - HX + 4 * gq + t;
-                    v[t] = xt < 0 ? lo : (xt > X - 1 ? hi : v[t]);
-                }
             }
             float out[4];
 #pragma unroll
@@ -403,7 +391,8 @@ struct SmoothXPass {
                     }
                 }
             }
-            // these generic-proxy writes come before the tensor copy that next refills the slot
+            // these generic-proxy writes come before the copy that next refills the buffer
+            // (a tensor copy writes through the async proxy)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
     }
@@ -417,14 +406,14 @@ struct SmoothXPass {
 // kernels, so that the block stays within 48 KB of shared memory).  Per slice step one block
 // barrier separates two independent halves: the x pass of the next slice (shared memory
 // to a double-buffered Gx) and the y pass of this slice (Gx to a per-thread register ring
-// of 2R + 1 slices that the z pass reads).  Columns outside [0, X) are read at the
-// clamped column (only tiles at the x edges take that path).  Each tap is one fused
-// multiply-add, acc = fma(w_k, g_k, acc), taken in the order k = -R..R for every axis.
-// Resident blocks per SM the kernel is held to: as many as its (2R + 1)-slice ring and,
-// in this variant, the per-value edge selects of the x pass allow without spilling much
-// (5 blocks are 48 registers a thread, 4 are 64, 3 are 85).
+// of 2R + 1 slices that the z pass reads).  On tiles at the x edges the R columns beyond
+// each edge are overwritten with the edge column in shared memory between two barriers
+// before the slice's x pass (the replicate boundary; SmoothXPass::fix_edges).  Each tap is
+// one fused multiply-add, acc = fma(w_k, g_k, acc), taken in the order k = -R..R for every
+// axis.  Resident blocks per SM the kernel is held to: as many as its (2R + 1)-slice ring
+// allows without spilling much (5 blocks are 48 registers a thread, 4 are 64, 3 are 85).
 template <int R>
-constexpr int kSmoothMinBlocksCp = R <= 3 ? 5 : (R <= 5 ? 4 : 3);
+constexpr int kSmoothMinBlocksCp = R <= 4 ? 5 : 4;
 
 template <int R>
 __global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel(SobIterArgs a) {
@@ -477,7 +466,14 @@ __global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel
         SmoothXPass<R> xp;  // staged rows are already the clamped rows
         xp.init([](int rr) { return rr * WS; });
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1]
-            xp.run(a, &G[k % NB][0][0][0], &Gx[k & 1][0][0][0], xedge, x0, X);
+            xp.run(a, &G[k % NB][0][0][0], &Gx[k & 1][0][0][0]);
+        };
+        // on a tile at an x edge: slice k's edge columns, after the barrier that made every
+        // thread's copies of it visible, and a second barrier before its x pass (block-uniform)
+        auto fix_edges = [&](int k) {
+            if (!xedge) return;
+            SmoothXPass<R>::fix_edges(&G[k % NB][0][0][0], x0, X);
+            __syncthreads();
         };
 
         // this thread's column; its momentum is loaded one output slice ahead
@@ -506,6 +502,7 @@ __global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel
         }
         cp_async_wait<NB - 1>();  // slice 0 has landed
         __syncthreads();
+        fix_edges(0);
         x_pass(0);
         for (int k = 0; k < nsl; ++k) {
             cp_async_wait<NB - 2>();  // slice k + 1 has landed (the later ones may not)
@@ -513,7 +510,10 @@ __global__ void __launch_bounds__(256, kSmoothMinBlocksCp<R>) sob_smooth3_kernel
                                       // and Gx[(k + 1) & 1] are no longer read
             stage(k + NB);            // into slice k's buffer
             cp_async_commit();
-            if (k + 1 < nsl) x_pass(k + 1);
+            if (k + 1 < nsl) {
+                fix_edges(k + 1);
+                x_pass(k + 1);
+            }
             // y pass of slice k for this thread's column, pushed into the z ring
 #pragma unroll
             for (int q = 0; q < K - 1; ++q) {
@@ -621,7 +621,7 @@ __global__ void __launch_bounds__(256, kSmoothMinBlocks<R>) sob_smooth3_tma_kern
             return (c * H + rs) * WS;
         });
         auto x_pass = [&](int k) {  // staged slice k -> Gx[k & 1] (its edge columns already fixed)
-            xp.run(a, &G[Ring::slot(nbase + (unsigned)k)][0], &Gx[k & 1][0][0][0], false, x0, X);
+            xp.run(a, &G[Ring::slot(nbase + (unsigned)k)][0], &Gx[k & 1][0][0][0]);
         };
         auto fix_edges = [&](int k) {  // after slice k has landed, before the barrier that precedes its x pass
             if (xedge) SmoothXPass<R>::fix_edges(&G[Ring::slot(nbase + (unsigned)k)][0], x0, X);
