@@ -271,6 +271,10 @@ size_t role_smem(int r, int variant = 0) {
     }
 }
 
+// threads per block and tile rows of kernel r's variant
+int role_threads(int r, int variant = 0) { return (r == R_PB && variant == 0) ? frg::kPassBThreads : 256; }
+int role_tile_y(int r, int variant = 0) { return (r == R_PB && variant == 0) ? frg::kPassBTileY : frg::kTileY; }
+
 typedef std::array<Shape, R_COUNT> Shapes;
 
 Shapes default_shapes(const fr_handle* h) {
@@ -297,7 +301,7 @@ int build_role(fr_handle* h, int r, Shape sh, cudaStream_t s = 0) {
     for (int p = 0; p < h->npairs; ++p) {
         const Pair& P = h->hpairs[p];
         for (int z0 = 0; z0 < P.Z; z0 += sh.depth)
-            for (int y0 = 0; y0 < P.Y; y0 += frg::kTileY)
+            for (int y0 = 0; y0 < P.Y; y0 += role_tile_y(r, sh.variant))
                 for (int x0 = 0; x0 < P.X; x0 += frg::kTileX) t.h.push_back(make_int4(p, x0, y0, z0));
     }
     if (t.h.size() > t.cap) return fail(h, FR_ERR_STATE, "tile table %d overflows (%zu > %zu)", r, t.h.size(), t.cap);
@@ -464,10 +468,11 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     auto add = [&](void** p, size_t bytes) { slots.push_back({p, bytes}); };
     add((void**)&h->d_pairs, sizeof(Pair) * n);
     add((void**)&h->d_tiles, sizeof(Tile) * ntiles);
-    // the solver kernels' tables, each with room for the shallowest tiles
+    // the solver kernels' tables, each with room for the shallowest and lowest tiles
     size_t cap = 0;
+    const int min_tile_y = std::min(frg::kTileY, frg::kPassBTileY);
     for (const Pair& P : h->hpairs)
-        cap += (size_t)((P.X + frg::kTileX - 1) / frg::kTileX) * ((P.Y + frg::kTileY - 1) / frg::kTileY) *
+        cap += (size_t)((P.X + frg::kTileX - 1) / frg::kTileX) * ((P.Y + min_tile_y - 1) / min_tile_y) *
                ((P.Z + kMinDepth - 1) / kMinDepth);
     for (int r : active_roles(h)) {
         h->ts[r].cap = cap;
@@ -555,7 +560,8 @@ int setup_cohort(fr_handle* h, const fr_pair* pairs, int n) {
     for (int r : active_roles(h))
         for (int v = 0; v < (has_tma_variant(r) ? 2 : 1); ++v) {
             int occ = 0;
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, role_fn(h, r, v), 256, role_smem(r, v)) !=
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, role_fn(h, r, v), role_threads(r, v),
+                                                              role_smem(r, v)) !=
                     cudaSuccess ||
                 occ < 1)
                 occ = 1;
@@ -631,7 +637,7 @@ int launch_ref_iter(fr_handle* h, int iter, float t, cudaStream_t s, cudaEvent_t
     if (h->ts[R_PB].shape.variant)
         frg::ref_pass_b_staged_kernel<<<h->ts[R_PB].grid, 256, frg::gather_staged_smem_bytes(), s>>>(a);
     else
-        frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, 256, 0, s>>>(a);
+        frg::ref_pass_b_kernel<<<h->ts[R_PB].grid, frg::kPassBThreads, 0, s>>>(a);
     if (ev) cudaEventRecord(ev[3], s);
     FR_LAUNCHED(h);
     return FR_OK;
@@ -875,7 +881,8 @@ int launch_role(fr_handle* h, int r, int iter, float t, cudaStream_t s) {
         args[0] = &sa;
     }
     const int v = h->ts[r].shape.variant;
-    FR_CUDA(h, cudaLaunchKernel(role_fn(h, r, v), dim3(h->ts[r].grid), dim3(256), args, role_smem(r, v), s));
+    FR_CUDA(h, cudaLaunchKernel(role_fn(h, r, v), dim3(h->ts[r].grid), dim3(role_threads(r, v)), args,
+                                role_smem(r, v), s));
     return FR_OK;
 }
 

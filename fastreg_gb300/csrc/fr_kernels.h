@@ -80,6 +80,8 @@ size_t ref_pass_a_smem_bytes();  // dynamic shared memory of ref_pass_a_kernel
 __global__ void ref_pass_a_kernel(RefIterArgs a);
 size_t ref_pass_a_tma_smem_bytes();  // dynamic shared memory of ref_pass_a_tma_kernel
 __global__ void ref_pass_a_tma_kernel(RefIterArgs a);
+// ref_pass_b_kernel runs 128-thread blocks on 32 x 4 tiles (its staged variant 256 on 32 x 8)
+constexpr int kPassBThreads = 128, kPassBTileY = 4;
 __global__ void ref_pass_b_kernel(RefIterArgs a);
 size_t gather_staged_smem_bytes();  // dynamic shared memory of the staged-gather pass B kernels
 __global__ void ref_pass_b_staged_kernel(RefIterArgs a);

@@ -681,8 +681,12 @@ __global__ void __launch_bounds__(256, 3) ref_pass_a_tma_kernel(RefIterArgs a) {
 
 // ----------------------------------------------------------------------------------
 // pass B: psi += alpha * v o psi, max update norm, convergence
+//
+// One thread per column of a 32 x 4 tile (128-thread blocks): the kernel waits on its
+// gathers, and 9 blocks of 128 threads at 56 registers hold 36 warps per SM where 256-thread
+// blocks held 32 (at 64 registers; at 48, for 5 blocks of 256, it spills).
 // ----------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256, 4) ref_pass_b_kernel(RefIterArgs a) {
+__global__ void __launch_bounds__(kPassBThreads, 9) ref_pass_b_kernel(RefIterArgs a) {
     __shared__ unsigned long long red[32];
     __shared__ bool last;
     const int tid = threadIdx.x;
